@@ -1,0 +1,642 @@
+// icp.cu -- colored ICP iteration (Park et al. 2017) for a batch of pairs.
+//
+// reference: color_icp::align (src/registration/color_icp.cu:151-234),
+// compute_JTJ_JTr_and_r_gauss_newton_functor
+// (src/registration/cuda_color_icp_build_least_square.cu:134-254) and
+// solve_JTJ_JTr<true> (src/registration/eigen_solver.hpp:44-85).
+//
+// One launch per Gauss-Newton iteration covers every pair.  A block owns a chunk
+// of one pair's source points: it transforms them by the pair's current pose,
+// finds the nearest target point inside max_corr (row-hashed grid, ties to the
+// smaller index), builds the geometric and photometric residuals and their
+// 6-vector Jacobians in FP32, and accumulates the 21 + 6 + 1 system terms plus
+// the correspondence count and squared distances.  Accumulation is compensated
+// FP32 inside the block (two-sum per thread and per shuffle level) and FP64 across
+// warps and blocks.  The last block of a pair to finish (atomic ticket, no
+// waiting) sums the pair's block partials in FP64 in block order, solves the 6x6
+// system by FP64 LDL^T, maps the step to SE(3) (Euler ZYX as the reference, or the
+// exponential), composes the pose in FP64 and applies the reference's
+// convergence test; a converged pair skips the remaining launches.  The source
+// cloud is never rewritten: the pose is applied on the fly.
+#include "grid_query.cuh"
+#include "icp.cuh"
+#include "stages.cuh"
+
+#include <algorithm>
+
+namespace gca3d
+{
+
+// ---------------------------------------------------------------------------
+// FP64 6x6 solve and pose maps (device; the oracle restates the same steps)
+// ---------------------------------------------------------------------------
+__device__ int solve6_device(const double *S /* 21 upper + 6 rhs */, double x[6])
+{
+    double A[6][6], b[6], D[6];
+    int perm[6];
+    int status = 0;
+    int u = 0;
+    for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j)
+        {
+            A[i][j] = A[j][i] = S[u];
+            ++u;
+        }
+    for (int i = 0; i < 6; ++i)
+    {
+        b[i] = -S[21 + i];
+        perm[i] = i;
+    }
+    for (int i = 0; i < 6; ++i)
+    {
+        if (!isfinite(b[i]))
+            status = 1;
+        for (int j = 0; j < 6; ++j)
+            if (!isfinite(A[i][j]))
+                status = 1;
+    }
+    if (status)
+    {
+        for (int i = 0; i < 6; ++i)
+            x[i] = 0.0;
+        return 1;
+    }
+    for (int k = 0; k < 6; ++k)
+    {
+        int piv = k;
+        for (int i = k + 1; i < 6; ++i)
+            if (fabs(A[i][i]) > fabs(A[piv][piv]))
+                piv = i;
+        if (piv != k)
+        {
+            for (int j = 0; j < 6; ++j)
+            {
+                double t = A[k][j];
+                A[k][j] = A[piv][j];
+                A[piv][j] = t;
+            }
+            for (int i = 0; i < 6; ++i)
+            {
+                double t = A[i][k];
+                A[i][k] = A[i][piv];
+                A[i][piv] = t;
+            }
+            int t = perm[k];
+            perm[k] = perm[piv];
+            perm[piv] = t;
+        }
+        D[k] = A[k][k];
+        if (fabs(D[k]) <= 2.2250738585072014e-308)
+        {
+            status = 1;
+            for (int i = k + 1; i < 6; ++i)
+                A[i][k] = 0.0;
+            continue;
+        }
+        for (int i = k + 1; i < 6; ++i)
+            A[i][k] /= D[k];
+        for (int i = k + 1; i < 6; ++i)
+            for (int j = k + 1; j <= i; ++j)
+            {
+                A[i][j] -= A[i][k] * A[j][k] * D[k];
+                A[j][i] = A[i][j];
+            }
+    }
+    double y[6], z[6];
+    for (int i = 0; i < 6; ++i)
+    {
+        double s = b[perm[i]];
+        for (int j = 0; j < i; ++j)
+            s -= A[i][j] * y[j];
+        y[i] = s;
+    }
+    for (int i = 0; i < 6; ++i)
+        y[i] = fabs(D[i]) > 2.2250738585072014e-308 ? y[i] / D[i] : 0.0;
+    for (int i = 5; i >= 0; --i)
+    {
+        double s = y[i];
+        for (int j = i + 1; j < 6; ++j)
+            s -= A[j][i] * z[j];
+        z[i] = s;
+    }
+    for (int i = 0; i < 6; ++i)
+        x[perm[i]] = z[i];
+    return status;
+}
+
+__device__ void pose_from_x_device(const double x[6], int map, double T[16])
+{
+    double R[3][3], t[3];
+    if (map == GCA3D_UPDATE_EULER_ZYX)
+    {
+        double sa, ca, sb, cb, sc, cc;
+        sincos(x[0], &sa, &ca);
+        sincos(x[1], &sb, &cb);
+        sincos(x[2], &sc, &cc);
+        R[0][0] = cc * cb;
+        R[0][1] = cc * sb * sa - sc * ca;
+        R[0][2] = cc * sb * ca + sc * sa;
+        R[1][0] = sc * cb;
+        R[1][1] = sc * sb * sa + cc * ca;
+        R[1][2] = sc * sb * ca - cc * sa;
+        R[2][0] = -sb;
+        R[2][1] = cb * sa;
+        R[2][2] = cb * ca;
+        t[0] = x[3], t[1] = x[4], t[2] = x[5];
+    }
+    else
+    {
+        const double w0 = x[0], w1 = x[1], w2 = x[2];
+        const double th2 = w0 * w0 + w1 * w1 + w2 * w2, th = sqrt(th2);
+        double A, B, C;
+        if (th < 1e-4)
+        {
+            A = 1.0 - th2 / 6.0 + th2 * th2 / 120.0;
+            B = 0.5 - th2 / 24.0 + th2 * th2 / 720.0;
+            C = 1.0 / 6.0 - th2 / 120.0 + th2 * th2 / 5040.0;
+        }
+        else
+        {
+            double s, c;
+            sincos(th, &s, &c);
+            A = s / th;
+            B = (1.0 - c) / th2;
+            C = (th - s) / (th2 * th);
+        }
+        const double K[3][3] = {{0, -w2, w1}, {w2, 0, -w0}, {-w1, w0, 0}};
+        double V[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+            {
+                double k2 = K[i][0] * K[0][j] + K[i][1] * K[1][j] + K[i][2] * K[2][j];
+                double I = i == j ? 1.0 : 0.0;
+                R[i][j] = I + A * K[i][j] + B * k2;
+                V[i][j] = I + B * K[i][j] + C * k2;
+            }
+        for (int i = 0; i < 3; ++i)
+            t[i] = V[i][0] * x[3] + V[i][1] * x[4] + V[i][2] * x[5];
+    }
+    for (int i = 0; i < 3; ++i)
+    {
+        for (int j = 0; j < 3; ++j)
+            T[4 * i + j] = R[i][j];
+        T[4 * i + 3] = t[i];
+    }
+    T[12] = T[13] = T[14] = 0.0;
+    T[15] = 1.0;
+}
+
+// ---------------------------------------------------------------------------
+// per-correspondence terms (cuda_color_icp_build_least_square.cu:184-253)
+// ---------------------------------------------------------------------------
+struct GNTerms
+{
+    float Jg[6], Jc[6];
+    float rg, rc;
+};
+
+__device__ __forceinline__ void gn_terms(float3 p, float Is, float3 q, float Iq, float3 n, float3 d, float slg,
+                                         float slc, GNTerms &o)
+{
+    const float rg_ = (p.x - q.x) * n.x + (p.y - q.y) * n.y + (p.z - q.z) * n.z;
+    o.Jg[0] = slg * (p.y * n.z - p.z * n.y);
+    o.Jg[1] = slg * (p.z * n.x - p.x * n.z);
+    o.Jg[2] = slg * (p.x * n.y - p.y * n.x);
+    o.Jg[3] = slg * n.x;
+    o.Jg[4] = slg * n.y;
+    o.Jg[5] = slg * n.z;
+    o.rg = slg * rg_;
+    // d^T (I - n n^T)
+    const float nd = n.x * d.x + n.y * d.y + n.z * d.z;
+    const float tx = d.x - nd * n.x, ty = d.y - nd * n.y, tz = d.z - nd * n.z;
+    o.Jc[0] = slc * (p.y * tz - p.z * ty);
+    o.Jc[1] = slc * (p.z * tx - p.x * tz);
+    o.Jc[2] = slc * (p.x * ty - p.y * tx);
+    o.Jc[3] = slc * tx;
+    o.Jc[4] = slc * ty;
+    o.Jc[5] = slc * tz;
+    // photometric residual on the tangent plane
+    const float px = p.x - rg_ * n.x, py = p.y - rg_ * n.y, pz = p.z - rg_ * n.z;
+    const float Iproj = Iq + (d.x * (px - q.x) + d.y * (py - q.y) + d.z * (pz - q.z));
+    o.rc = slc * (Iproj - Is);
+}
+
+// accumulator of kTerms values: plain FP32 or FP32 value + FP32 error (two-sum)
+template <bool Comp> struct Acc
+{
+    float s[kTerms];
+    float e[kTerms];
+    __device__ void zero()
+    {
+#pragma unroll
+        for (int k = 0; k < kTerms; ++k)
+            s[k] = 0.0f, e[k] = 0.0f;
+    }
+    __device__ __forceinline__ void add(int k, float x)
+    {
+        if (Comp)
+        {
+            const float t = s[k] + x;
+            const float bp = t - s[k];
+            e[k] += (s[k] - (t - bp)) + (x - bp);
+            s[k] = t;
+        }
+        else
+            s[k] += x;
+    }
+    __device__ __forceinline__ void add_terms(const GNTerms &o, float d2)
+    {
+        int u = 0;
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+#pragma unroll
+            for (int b = a; b < 6; ++b)
+                add(u++, o.Jg[a] * o.Jg[b] + o.Jc[a] * o.Jc[b]);
+#pragma unroll
+        for (int a = 0; a < 6; ++a)
+            add(21 + a, o.Jg[a] * o.rg + o.Jc[a] * o.rc);
+        add(27, o.rg * o.rg + o.rc * o.rc);
+        add(28, 1.0f);
+        add(29, d2);
+    }
+    // warp reduction; result valid in lane 0
+    __device__ __forceinline__ void warp_reduce()
+    {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+#pragma unroll
+            for (int k = 0; k < kTerms; ++k)
+            {
+                const float s2 = __shfl_down_sync(0xffffffffu, s[k], o);
+                if (Comp)
+                {
+                    const float e2 = __shfl_down_sync(0xffffffffu, e[k], o);
+                    const float t = s[k] + s2;
+                    const float bp = t - s[k];
+                    e[k] += e2 + ((s[k] - (t - bp)) + (s2 - bp));
+                    s[k] = t;
+                }
+                else
+                    s[k] += s2;
+            }
+        }
+    }
+    __device__ __forceinline__ double value(int k) const
+    {
+        return Comp ? (double)s[k] + (double)e[k] : (double)s[k];
+    }
+};
+
+// sum of the block's kTerms values into part[kTerms] (FP64 across warps when
+// compensated, FP32 otherwise); all threads must call
+template <bool Comp>
+__device__ __forceinline__ void block_reduce_store(Acc<Comp> &acc, double *part)
+{
+    __shared__ double s_w[kIcpThreads / 32][kTerms];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    acc.warp_reduce();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < kTerms; ++k)
+            s_w[warp][k] = acc.value(k);
+    __syncthreads();
+    if (threadIdx.x < kTerms)
+    {
+        if (Comp)
+        {
+            double v = 0.0;
+            for (int w = 0; w < kIcpThreads / 32; ++w)
+                v += s_w[w][threadIdx.x];
+            part[threadIdx.x] = v;
+        }
+        else
+        {
+            float v = 0.0f;
+            for (int w = 0; w < kIcpThreads / 32; ++w)
+                v += (float)s_w[w][threadIdx.x];
+            part[threadIdx.x] = (double)v;
+        }
+    }
+}
+
+__device__ __forceinline__ int find_pair(const int *bmap, int P, int b)
+{
+    if (b >= bmap[P])
+        return -1;
+    int lo = 0, hi = P - 1;
+    while (lo < hi)
+    {
+        int mid = (lo + hi + 1) >> 1;
+        if (bmap[mid] <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// per-scale setup: block map, per-pair counts, reset of the per-scale flags
+__global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
+                            int chunk, int first_scale)
+{
+    if (threadIdx.x != 0)
+        return;
+    int b = 0;
+    for (int p = 0; p < P; ++p)
+    {
+        PairState &S = st[p];
+        const int ns = src_off[p + 1] - src_off[p];
+        const int nt = tgt_off[p + 1] - tgt_off[p];
+        const int nb = (ns > 0 && nt > 0) ? (ns + chunk - 1) / chunk : 0;
+        bmap[p] = b;
+        b += nb;
+        S.nblocks = nb;
+        S.nsrc = ns;
+        S.ntgt = nt;
+        S.ticket = 0;
+        S.active = nb > 0 ? 1 : 0;
+        S.converged = 0;
+        if (first_scale)
+        {
+            S.iters = 0;
+            S.status = 0;
+        }
+        if (nb == 0)
+        {
+            S.status = GCA3D_ERR_NO_CORRESPONDENCES;
+            S.rmse_ref = S.fitness = S.inlier_rmse = 0.0;
+        }
+    }
+    bmap[P] = b;
+}
+
+__global__ void k_state_init(PairState *st, int P, const double *T_init)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P)
+        return;
+    for (int k = 0; k < 16; ++k)
+        st[p].T[k] = T_init ? T_init[16 * p + k] : (k % 5 == 0 ? 1.0 : 0.0);
+    st[p].iters = 0;
+    st[p].status = 0;
+    st[p].rmse_ref = st[p].fitness = st[p].inlier_rmse = 0.0;
+}
+
+template <bool Comp>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_iter(const float4 *__restrict__ src_pos, const int32_t *src_off,
+                                                          GridDev g, const float4 *__restrict__ attr0,
+                                                          const float4 *__restrict__ attr1, PairState *st,
+                                                          const int *bmap, int P, double *partials, IcpScale prm,
+                                                          int32_t *nn_out)
+{
+    __shared__ int s_pair;
+    __shared__ float s_T[12];
+    __shared__ int s_last;
+    if (threadIdx.x == 0)
+    {
+        int p = find_pair(bmap, P, blockIdx.x);
+        if (p >= 0 && !st[p].active)
+            p = -1;
+        s_pair = p;
+        if (p >= 0)
+            for (int k = 0; k < 12; ++k)
+                s_T[k] = (float)st[p].T[k];
+    }
+    __syncthreads();
+    const int pair = s_pair;
+    if (pair < 0)
+        return;
+    const KeyLayout L = *g.layout;
+    const float3 o = g.gmin[pair];
+    const int bstart = bmap[pair];
+    const int start = src_off[pair] + (blockIdx.x - bstart) * kIcpChunk;
+    const int end = min(start + kIcpChunk, src_off[pair + 1]);
+    const int tbase = g.seg_off[pair];
+    const float rr = __fmul_rn(prm.max_corr, prm.max_corr);
+    Acc<Comp> acc;
+    acc.zero();
+    for (int i = start + threadIdx.x; i < end; i += kIcpThreads)
+    {
+        const float4 s4 = src_pos[i];
+        const float3 p = make_float3(s_T[0] * s4.x + s_T[1] * s4.y + s_T[2] * s4.z + s_T[3],
+                                     s_T[4] * s4.x + s_T[5] * s4.y + s_T[6] * s4.z + s_T[7],
+                                     s_T[8] * s4.x + s_T[9] * s4.y + s_T[10] * s4.z + s_T[11]);
+        const NNBest best = nn_search_one(g, L, pair, o, p, rr);
+        if (nn_out)
+            nn_out[i] = best.t >= 0 ? __ldg(&g.sidx[best.t]) - tbase : -1;
+        if (best.t < 0)
+            continue;
+        const float4 q = __ldg(&g.spos[best.t]);
+        const float4 a0 = __ldg(&attr0[best.t]);
+        const float4 a1 = __ldg(&attr1[best.t]);
+        GNTerms terms;
+        gn_terms(p, s4.w, make_float3(q.x, q.y, q.z), a0.w, make_float3(a0.x, a0.y, a0.z),
+                 make_float3(a1.x, a1.y, a1.z), prm.sqrt_lg, prm.sqrt_lc, terms);
+        acc.add_terms(terms, best.d2);
+    }
+    block_reduce_store<Comp>(acc, partials + (size_t)blockIdx.x * kTermsPad);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const unsigned t = atomicAdd(&st[pair].ticket, 1u);
+        s_last = (int)t == st[pair].nblocks - 1;
+    }
+    __syncthreads();
+    if (!s_last)
+        return;
+    // ---- last block of the pair: reduce the partials in block order --------
+    __shared__ double s_red[kIcpThreads / 32][kTermsPad];
+    const int nb = st[pair].nblocks;
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    if (lane < kTerms)
+    {
+        double v = 0.0;
+        float vf = 0.0f;
+        for (int j = grp; j < nb; j += kIcpThreads / 32)
+        {
+            const double x = __ldcg(partials + (size_t)(bstart + j) * kTermsPad + lane);
+            if (Comp)
+                v += x;
+            else
+                vf += (float)x;
+        }
+        s_red[grp][lane] = Comp ? v : (double)vf;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double S[kTerms];
+        for (int k = 0; k < kTerms; ++k)
+        {
+            double v = 0.0;
+            float vf = 0.0f;
+            for (int w = 0; w < kIcpThreads / 32; ++w)
+            {
+                if (Comp)
+                    v += s_red[w][k];
+                else
+                    vf += (float)s_red[w][k];
+            }
+            S[k] = Comp ? v : (double)vf;
+        }
+        PairState &Ps = st[pair];
+        const double ns = (double)Ps.nsrc;
+        Ps.rmse_ref = S[27] / ns;
+        Ps.fitness = S[28] / ns;
+        Ps.inlier_rmse = S[28] > 0.0 ? sqrt(S[29] / S[28]) : 0.0;
+        double x[6], Ti[16];
+        const int singular = solve6_device(S, x);
+        if (S[28] == 0.0)
+            Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
+        else if (singular && Ps.status == 0)
+            Ps.status = GCA3D_ERR_SINGULAR;
+        pose_from_x_device(x, prm.update_map, Ti);
+        double Tn[16];
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c)
+            {
+                double v = 0.0;
+                for (int k = 0; k < 4; ++k)
+                    v += Ti[4 * r + k] * Ps.T[4 * k + c];
+                Tn[4 * r + c] = v;
+            }
+        for (int k = 0; k < 16; ++k)
+            Ps.T[k] = Tn[k];
+        Ps.iters += 1;
+        // convergence test of color_icp.cu:216-228 on this step
+        const double cth = 0.5 * (Ti[0] + Ti[5] + Ti[10] - 1.0);
+        const double tsq = Ti[3] * Ti[3] + Ti[7] * Ti[7] + Ti[11] * Ti[11];
+        if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
+        {
+            Ps.converged = 1;
+            Ps.active = 0;
+        }
+        Ps.ticket = 0;
+    }
+}
+
+int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
+              bool first_scale)
+{
+    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, kIcpChunk, first_scale ? 1 : 0);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit)
+{
+    k_state_init<<<grid_for(P, 128), 128, 0, ctx->stream>>>(st, P, d_Tinit);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
+                  PairState *st, const int *bmap, int max_blocks, double *partials, const IcpScale &prm,
+                  bool compensated, int32_t *nn_out)
+{
+    if (compensated)
+        k_icp_iter<true><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, attr0, attr1, st,
+                                                                      bmap, src.P, partials, prm, nn_out);
+    else
+        k_icp_iter<false><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, attr0, attr1, st,
+                                                                       bmap, src.P, partials, prm, nn_out);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// system for given correspondences (cuda_build_gauss_newton_color_icp) and the
+// per-point |r_g| + |r_c| (cuda_compute_abs_residual_color_icp)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kIcpThreads) k_build_gn(const float4 *__restrict__ sp, const int32_t *d_ns,
+                                                          const float4 *__restrict__ tp, const float4 *__restrict__ tn,
+                                                          const float4 *__restrict__ tg, const int32_t *nn,
+                                                          float slg, float slc, double *partials,
+                                                          unsigned *ticket, double *out)
+{
+    const int ns = *d_ns;
+    Acc<true> acc;
+    acc.zero();
+    for (int i = blockIdx.x * kIcpThreads + threadIdx.x; i < ns; i += gridDim.x * kIcpThreads)
+    {
+        const int j = nn[i];
+        if (j < 0)
+            continue;
+        const float4 s4 = sp[i], q = tp[j], n = tn[j], d = tg[j];
+        GNTerms t;
+        gn_terms(make_float3(s4.x, s4.y, s4.z), s4.w, make_float3(q.x, q.y, q.z), q.w, make_float3(n.x, n.y, n.z),
+                 make_float3(d.x, d.y, d.z), slg, slc, t);
+        const float dx = q.x - s4.x, dy = q.y - s4.y, dz = q.z - s4.z;
+        acc.add_terms(t, dx * dx + dy * dy + dz * dz);
+    }
+    block_reduce_store<true>(acc, partials + (size_t)blockIdx.x * kTermsPad);
+    __threadfence();
+    __syncthreads();
+    __shared__ int s_last;
+    if (threadIdx.x == 0)
+        s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last)
+        return;
+    if (threadIdx.x < kTerms)
+    {
+        double v = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b)
+            v += __ldcg(partials + (size_t)b * kTermsPad + threadIdx.x);
+        out[threadIdx.x] = v;
+    }
+    if (threadIdx.x == 0)
+        *ticket = 0;
+}
+
+__global__ void k_abs_residual(const float4 *__restrict__ sp, const int32_t *d_ns, const float4 *__restrict__ tp,
+                               const float4 *__restrict__ tn, const float4 *__restrict__ tg, const int32_t *nn,
+                               float slg, float slc, float *out)
+{
+    const int ns = *d_ns;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x)
+    {
+        const int j = nn[i];
+        if (j < 0)
+        {
+            out[i] = 0.0f;
+            continue;
+        }
+        const float4 s4 = sp[i], q = tp[j], n = tn[j], d = tg[j];
+        GNTerms t;
+        gn_terms(make_float3(s4.x, s4.y, s4.z), s4.w, make_float3(q.x, q.y, q.z), q.w, make_float3(n.x, n.y, n.z),
+                 make_float3(d.x, d.y, d.z), slg, slc, t);
+        out[i] = fabsf(t.rg) + fabsf(t.rc);
+    }
+}
+
+int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
+             double *out30)
+{
+    const int blocks = std::min(grid_for(src->capacity, kIcpThreads * 4), ctx->num_sms * 2);
+    double *partials = ctx->arena.get<double>((size_t)blocks * kTermsPad);
+    unsigned *ticket = ctx->arena.get<unsigned>(1);
+    double *d_out = ctx->arena.get<double>(kTermsPad);
+    if (!partials || !ticket || !d_out)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "build_gn: scratch");
+    GCA_CUDA(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream));
+    k_build_gn<<<blocks, kIcpThreads, 0, ctx->stream>>>(src->pos, src->d_count, tgt->pos, tgt->nrm, tgt->grd, nn,
+                                                        sqrtf(lambda), sqrtf(1.0f - lambda), partials, ticket, d_out);
+    GCA_CHECK_LAUNCH(ctx);
+    GCA_CUDA(ctx, cudaMemcpyAsync(out30, d_out, sizeof(double) * kTerms, cudaMemcpyDeviceToHost, ctx->stream));
+    GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GCA3D_OK;
+}
+
+int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
+                 float *out)
+{
+    k_abs_residual<<<grid_for(src->capacity), kBlock, 0, ctx->stream>>>(
+        src->pos, src->d_count, tgt->pos, tgt->nrm, tgt->grd, nn, sqrtf(lambda), sqrtf(1.0f - lambda), out);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+} // namespace gca3d

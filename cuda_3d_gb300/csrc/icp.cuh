@@ -1,0 +1,47 @@
+// icp.cuh -- per-pair device state and per-scale parameters of the ICP kernels.
+#pragma once
+
+#include "stages.cuh"
+
+namespace gca3d
+{
+
+constexpr int kIcpThreads = 256;
+constexpr int kIcpChunk = 1024; // source points per block
+constexpr int kTerms = 30;      // 21 JTJ (upper) + 6 JTr + r^2 + correspondences + sum d^2
+constexpr int kTermsPad = 32;
+
+struct PairState
+{
+    double T[16];
+    double rmse_ref, fitness, inlier_rmse;
+    int iters;
+    int converged;
+    int active;
+    int status;
+    unsigned int ticket;
+    int nblocks;
+    int nsrc;
+    int ntgt;
+};
+
+struct IcpScale
+{
+    float max_corr;
+    float sqrt_lg, sqrt_lc;
+    int update_map;
+    double rot_eps, trans_eps;
+};
+
+int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit);
+int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
+              bool first_scale);
+int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
+                  PairState *st, const int *bmap, int max_blocks, double *partials, const IcpScale &prm,
+                  bool compensated, int32_t *nn_out);
+int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
+             double *out30);
+int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
+                 float *out);
+
+} // namespace gca3d

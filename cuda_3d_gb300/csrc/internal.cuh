@@ -1,0 +1,280 @@
+// internal.cuh -- shared types and device helpers of the gca3d library.
+#pragma once
+
+#include "gca3d.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace gca3d
+{
+
+// ---------------------------------------------------------------------------
+// limits
+// ---------------------------------------------------------------------------
+constexpr int kMaxSegments = 4096;       // pairs / clouds in one batched stage
+constexpr int kBlock = 256;              // threads per block for streaming kernels
+constexpr uint32_t kSpinLimit = 1u << 22; // polls before a look-back gives up
+
+// device error word bits
+enum : int
+{
+    kErrTimeout = 1,
+    kErrCapacity = 2,
+    kErrKeyBits = 4,
+    kErrSingular = 8,
+    kErrInvalid = 16,
+};
+
+// ---------------------------------------------------------------------------
+// scratch memory: chunked bump allocator, reset per top-level call.  A replay
+// of the same sequence of requests returns the same addresses, which is what
+// graph capture relies on.
+// ---------------------------------------------------------------------------
+struct Arena
+{
+    struct Chunk
+    {
+        char *ptr = nullptr;
+        size_t size = 0, used = 0;
+    };
+    std::vector<Chunk> chunks;
+    size_t cur = 0;
+    bool frozen = false; // no growth allowed (during capture)
+    bool failed = false;
+
+    void *take(size_t bytes);
+    void reset()
+    {
+        for (auto &c : chunks)
+            c.used = 0;
+        cur = 0;
+        failed = false;
+    }
+    void release();
+    void swap(Arena &o)
+    {
+        chunks.swap(o.chunks);
+        std::swap(cur, o.cur);
+        std::swap(frozen, o.frozen);
+        std::swap(failed, o.failed);
+    }
+    Arena() = default;
+    Arena(const Arena &) = delete;
+    Arena &operator=(const Arena &) = delete;
+    ~Arena() { release(); }
+    template <typename T> T *get(size_t count) { return static_cast<T *>(take(count * sizeof(T))); }
+};
+
+} // namespace gca3d
+
+// ---------------------------------------------------------------------------
+// opaque handles
+// ---------------------------------------------------------------------------
+struct gca3d_context
+{
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+    gca3d::Arena arena;
+    int *d_err = nullptr;  // device error word
+    int *h_pinned = nullptr; // pinned scratch for small read-backs (64 ints)
+    int64_t launches = 0;
+    std::string last_error;
+};
+
+struct gca3d_cloud
+{
+    int64_t capacity = 0;
+    float4 *pos = nullptr; // x, y, z, intensity
+    float4 *col = nullptr; // r, g, b, 0
+    float4 *nrm = nullptr;
+    float4 *grd = nullptr;
+    int32_t *d_count = nullptr;
+    bool has_normals = false;
+    bool has_grad = false;
+    float grad_radius = 0.0f;
+    int device = 0;
+};
+
+namespace gca3d
+{
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+int fail(gca3d_context *ctx, int status, const std::string &msg);
+int cuda_fail(gca3d_context *ctx, cudaError_t e, const char *where);
+#define GCA_CUDA(ctx, call)                                                                        \
+    do                                                                                             \
+    {                                                                                              \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return ::gca3d::cuda_fail((ctx), e_, #call);                                           \
+    } while (0)
+#define GCA_CHECK_LAUNCH(ctx)                                                                      \
+    do                                                                                             \
+    {                                                                                              \
+        (ctx)->launches++;                                                                         \
+        cudaError_t e_ = cudaGetLastError();                                                       \
+        if (e_ != cudaSuccess)                                                                     \
+            return ::gca3d::cuda_fail((ctx), e_, __func__);                                        \
+    } while (0)
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+inline int grid_for(int64_t n, int per_block = kBlock)
+{
+    int g = div_up(n > 0 ? n : 1, per_block);
+    return g > 0 ? g : 1;
+}
+int ensure_attr(gca3d_context *ctx, gca3d_cloud *c, bool normals, bool grad);
+// reads and clears the device error word; maps bits to a status
+int consume_device_error(gca3d_context *ctx, const char *where);
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+
+// colour -> intensity in FP64 then rounded, without contraction, as
+// color3::to_intensity (src/geometry/type.hpp:45-51)
+__device__ __forceinline__ float intensity_of(float r, float g, float b)
+{
+    double s = __dadd_rn(__dmul_rn(0.2126, (double)r), __dmul_rn(0.7152, (double)g));
+    s = __dadd_rn(s, __dmul_rn(0.0722, (double)b));
+    return (float)s;
+}
+
+// float <-> order-preserving int (for atomicMin/atomicMax on floats)
+__device__ __forceinline__ int float_to_ordered(float f)
+{
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float ordered_to_float(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+inline float ordered_to_float_host(int i)
+{
+    int j = i >= 0 ? i : i ^ 0x7FFFFFFF;
+    float f;
+    memcpy(&f, &j, 4);
+    return f;
+}
+
+// squared distance q - p, unfused, the reference's order (cuda_nn_search.cu:195-200)
+__device__ __forceinline__ float dist2_ref(float qx, float qy, float qz, float px, float py, float pz)
+{
+    float dx = __fsub_rn(qx, px), dy = __fsub_rn(qy, py), dz = __fsub_rn(qz, pz);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// floor((p - mn) / cell), IEEE sub and div (cuda_voxel_grid_down_sample.cu:40-45)
+__device__ __forceinline__ int cell_of(float p, float mn, float cell)
+{
+    return __float2int_rd(__fdiv_rn(__fsub_rn(p, mn), cell));
+}
+
+__device__ __forceinline__ int bitlen_u32(uint32_t v) { return v ? 32 - __clz(v) : 0; }
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// bounded spin read of a volatile 64-bit status word until pred holds
+__device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long *p)
+{
+    return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+
+// ---------------------------------------------------------------------------
+// batched ("segmented") point sets: P clouds back to back
+// ---------------------------------------------------------------------------
+
+// per-segment AABB as ordered ints: [seg][0..2] min, [seg][3..5] max
+struct SegBounds
+{
+    int *ord; // 6 * P
+};
+
+// parameters of one packed 64-bit cell key layout, shared by all segments
+struct KeyLayout
+{
+    int bseg, bx, by, bz; // bits per field; key = seg|cx|cy|cz from MSB to LSB
+    int total_bits;
+};
+
+// a grid over the target segments
+struct GridDev
+{
+    // per segment
+    float3 *gmin;  // grid origin
+    float cell;    // cell edge
+    KeyLayout *layout;
+    // sorted points (global positions over all segments)
+    float4 *spos;  // x, y, z, __int_as_float(cz)
+    int32_t *sidx; // batch index of the point (original order)
+    float *sint;   // intensity in sorted order
+    uint64_t *skey;
+    // row hash: key = (seg, cx, cy) -> [start, end)
+    unsigned long long *hkeys;
+    int2 *hvals;
+    uint32_t hmask;
+    const int32_t *seg_off; // [P + 1] offsets of the segments in the sorted arrays
+};
+
+constexpr unsigned long long kEmptyKey = ~0ull;
+
+__device__ __forceinline__ uint32_t hash_u64(unsigned long long k)
+{
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (uint32_t)k;
+}
+
+__device__ __forceinline__ int2 row_lookup(const unsigned long long *hkeys, const int2 *hvals,
+                                           uint32_t hmask, unsigned long long rk)
+{
+    uint32_t h = hash_u64(rk) & hmask;
+    for (uint32_t probe = 0; probe <= hmask; ++probe)
+    {
+        unsigned long long k = __ldg(hkeys + h);
+        if (k == rk)
+            return __ldg(hvals + h);
+        if (k == kEmptyKey)
+            break;
+        h = (h + 1) & hmask;
+    }
+    return make_int2(0, 0);
+}
+
+// ---------------------------------------------------------------------------
+// stage entry points implemented in the .cu files (all stream-ordered)
+// ---------------------------------------------------------------------------
+
+// radix sort of (key, value) pairs by the low `max_bits` bits, n on the device.
+// keys/vals are ping-pong buffers of capacity `cap`; on return *result_in_alt
+// (device int) says whether the sorted data is in the alternate buffers.
+struct SortBuffers
+{
+    uint64_t *keys[2];
+    int32_t *vals[2];
+    int *d_sel; // device: index of the buffer holding the sorted data
+};
+int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t cap, int max_bits,
+               const int *d_key_bits /* device: bits actually used, or nullptr */);
+
+// exclusive scan of int32 values (n on the device), writes total to *d_total
+int exclusive_scan(gca3d_context *ctx, const int32_t *in, int32_t *out, const int32_t *d_n,
+                   int64_t cap, int32_t *d_total);
+
+} // namespace gca3d

@@ -1,0 +1,357 @@
+// normals.cu -- fused PCA normals and colour gradients over a grid's own points.
+//
+// reference: cuda_estimate_normals (src/geometry/cuda_estimate_normals.cu:46-199) and
+// compute_color_gradient_functor (src/registration/cuda_compute_color_gradient.cu:13-90).
+//
+// The reference materialises CSR neighbour lists, expands them to per-neighbour
+// moment vectors and reduces by key.  Here one thread walks its 27-cell
+// neighbourhood in the grid (points already in cell order) and accumulates in
+// registers; no lists exist.  Moments are taken about the query point, so the
+// FP32 covariance does not cancel at metre-scale coordinates (the reference's
+// E[xx^T] - E[x]E[x]^T does).  The 3x3 eigen-problem is solved in closed form in
+// FP32; when the two smallest eigenvalues are close the covariance is rebuilt in
+// FP64 and solved by Jacobi rotations.  The gradient follows the reference's
+// system: tangent-plane least squares, (knn - 1)^2 n n^T orthogonality term,
+// 1e-6 ridge, LDL^T solve (in the tangent/normal basis, see solve_gradient_system).
+#include "grid_query.cuh"
+#include "stages.cuh"
+
+#include <algorithm>
+
+namespace gca3d
+{
+
+constexpr int kMaxNN = 64;
+
+// FP64 Jacobi eigenvector of the smallest eigenvalue (same sweeps as the oracle)
+__device__ void jacobi_smallest(double a[3][3], double out[3])
+{
+    double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int sweep = 0; sweep < 64; ++sweep)
+    {
+        double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+        double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+        if (off <= 1e-36 * diag || off == 0.0)
+            break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q)
+            {
+                if (a[p][q] == 0.0)
+                    continue;
+                double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; ++k)
+                {
+                    double akp = a[k][p], akq = a[k][q];
+                    a[k][p] = c * akp - s * akq;
+                    a[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k)
+                {
+                    double apk = a[p][k], aqk = a[q][k];
+                    a[p][k] = c * apk - s * aqk;
+                    a[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k)
+                {
+                    double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    int s = 0;
+    for (int k = 1; k < 3; ++k)
+        if (a[k][k] < a[s][s])
+            s = k;
+    double l = sqrt(V[0][s] * V[0][s] + V[1][s] * V[1][s] + V[2][s] * V[2][s]);
+    out[0] = V[0][s] / l;
+    out[1] = V[1][s] / l;
+    out[2] = V[2][s] / l;
+}
+
+// closed-form symmetric 3x3 eigen-system (trigonometric eigenvalues, eigenvector
+// of the smallest one from cross products of the rows of A - lambda I).
+// Returns false when the smallest eigenvalue is not well separated.
+__device__ bool smallest_eigvec_f32(float a00, float a01, float a02, float a11, float a12, float a22, float3 &n)
+{
+    float m = fmaxf(fmaxf(fmaxf(fabsf(a00), fabsf(a01)), fmaxf(fabsf(a02), fabsf(a11))), fmaxf(fabsf(a12), fabsf(a22)));
+    if (!(m > 0.0f))
+        return false;
+    const float inv = 1.0f / m;
+    a00 *= inv, a01 *= inv, a02 *= inv, a11 *= inv, a12 *= inv, a22 *= inv;
+    const float q = (a00 + a11 + a22) * (1.0f / 3.0f);
+    const float b00 = a00 - q, b11 = a11 - q, b22 = a22 - q;
+    const float off = a01 * a01 + a02 * a02 + a12 * a12;
+    const float p2 = (b00 * b00 + b11 * b11 + b22 * b22 + 2.0f * off) * (1.0f / 6.0f);
+    if (!(p2 > 0.0f))
+        return false;
+    const float p = sqrtf(p2);
+    const float det = b00 * (b11 * b22 - a12 * a12) - a01 * (a01 * b22 - a12 * a02) + a02 * (a01 * a12 - b11 * a02);
+    float r = det / (2.0f * p2 * p);
+    r = fminf(fmaxf(r, -1.0f), 1.0f);
+    const float phi = acosf(r) * (1.0f / 3.0f);
+    const float lmax = q + 2.0f * p * cosf(phi);
+    const float lmin = q + 2.0f * p * cosf(phi + 2.0943951023931957f);
+    const float lmid = 3.0f * q - lmax - lmin;
+    if (!(lmid - lmin > 1e-2f * (lmax - lmin)))
+        return false;
+    const float3 r0 = make_float3(a00 - lmin, a01, a02);
+    const float3 r1 = make_float3(a01, a11 - lmin, a12);
+    const float3 r2 = make_float3(a02, a12, a22 - lmin);
+    const float3 c0 = make_float3(r0.y * r1.z - r0.z * r1.y, r0.z * r1.x - r0.x * r1.z, r0.x * r1.y - r0.y * r1.x);
+    const float3 c1 = make_float3(r0.y * r2.z - r0.z * r2.y, r0.z * r2.x - r0.x * r2.z, r0.x * r2.y - r0.y * r2.x);
+    const float3 c2 = make_float3(r1.y * r2.z - r1.z * r2.y, r1.z * r2.x - r1.x * r2.z, r1.x * r2.y - r1.y * r2.x);
+    const float d0 = c0.x * c0.x + c0.y * c0.y + c0.z * c0.z;
+    const float d1 = c1.x * c1.x + c1.y * c1.y + c1.z * c1.z;
+    const float d2 = c2.x * c2.x + c2.y * c2.y + c2.z * c2.z;
+    float3 c = c0;
+    float d = d0;
+    if (d1 > d)
+        c = c1, d = d1;
+    if (d2 > d)
+        c = c2, d = d2;
+    if (!(d > 1e-20f))
+        return false;
+    const float il = rsqrtf(d);
+    n = make_float3(c.x * il, c.y * il, c.z * il);
+    return true;
+}
+
+// LDL^T solve of a symmetric 3x3 (little_3x3_ldlt_solve.cuh:6-67 factorisation)
+__device__ __forceinline__ float3 ldlt3(float A00, float A01, float A02, float A11, float A12, float A22, float b0,
+                                        float b1, float b2)
+{
+    const float D0 = A00, L10 = A01 / D0, L20 = A02 / D0;
+    const float D1 = A11 - L10 * L10 * D0;
+    const float L21 = (A12 - L10 * L20 * D0) / D1;
+    const float D2 = A22 - L20 * L20 * D0 - L21 * L21 * D1;
+    float x0 = b0, x1 = b1 - L10 * x0, x2 = b2 - L20 * x0 - L21 * x1;
+    x0 /= D0, x1 /= D1, x2 /= D2;
+    x1 -= L21 * x2;
+    x0 -= L10 * x1 + L20 * x2;
+    return make_float3(x0, x1, x2);
+}
+
+// The colour-gradient system of compute_color_gradient_functor
+// (cuda_compute_color_gradient.cu:57-88):  (sum v v^T + w n n^T + 1e-6 I) d = sum v dI
+// with w = (knn - 1)^2.  The w n n^T term is ~1e4-1e5 times the tangent entries, so
+// the xyz-basis LDL^T loses most FP32 digits.  The same system is solved in the
+// orthonormal basis (t1, t2, n): there the large term sits on the last diagonal
+// entry only and the tangent block factors first, at full FP32 accuracy.
+__device__ __forceinline__ float3 solve_gradient_system(float A00, float A01, float A02, float A11, float A12,
+                                                        float A22, float b0, float b1, float b2, float3 n, float w)
+{
+    const float nn = n.x * n.x + n.y * n.y + n.z * n.z;
+    if (!(nn > 0.0f))
+        return ldlt3(A00 + 1.0e-6f, A01, A02, A11 + 1.0e-6f, A12, A22 + 1.0e-6f, b0, b1, b2);
+    float3 t1;
+    if (fabsf(n.x) > fabsf(n.y))
+    {
+        const float il = rsqrtf(n.x * n.x + n.z * n.z);
+        t1 = make_float3(-n.z * il, 0.0f, n.x * il);
+    }
+    else
+    {
+        const float il = rsqrtf(n.y * n.y + n.z * n.z);
+        t1 = make_float3(0.0f, n.z * il, -n.y * il);
+    }
+    const float3 t2 = make_float3(n.y * t1.z - n.z * t1.y, n.z * t1.x - n.x * t1.z, n.x * t1.y - n.y * t1.x);
+    const float3 e[3] = {t1, t2, n};
+    float3 Ae[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        Ae[k] = make_float3(A00 * e[k].x + A01 * e[k].y + A02 * e[k].z, A01 * e[k].x + A11 * e[k].y + A12 * e[k].z,
+                            A02 * e[k].x + A12 * e[k].y + A22 * e[k].z);
+    auto dot3 = [](float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; };
+    const float m00 = dot3(e[0], Ae[0]) + 1.0e-6f, m01 = dot3(e[0], Ae[1]), m02 = dot3(e[0], Ae[2]);
+    const float m11 = dot3(e[1], Ae[1]) + 1.0e-6f, m12 = dot3(e[1], Ae[2]);
+    const float m22 = dot3(e[2], Ae[2]) + w * nn + 1.0e-6f;
+    const float3 b = make_float3(b0, b1, b2);
+    const float3 y = ldlt3(m00, m01, m02, m11, m12, m22, dot3(e[0], b), dot3(e[1], b), dot3(e[2], b));
+    return make_float3(y.x * t1.x + y.y * t2.x + y.z * n.x, y.x * t1.y + y.y * t2.y + y.z * n.y,
+                       y.x * t1.z + y.y * t2.z + y.z * n.z);
+}
+
+struct NbrEntry
+{
+    float d2;
+    int idx; // batch index (original order)
+    int t;   // grid position
+};
+
+__global__ void __launch_bounds__(256) k_normals_grad(GridDev g, const int32_t *d_n, int do_normals, float rn,
+                                                      int max_nn, int do_grad, float rg, const float4 *in_nrm,
+                                                      float4 *attr0, float4 *attr1, float4 *nrm_out,
+                                                      float4 *grd_out)
+{
+    const int n = *d_n;
+    const KeyLayout L = *g.layout;
+    const int segshift = L.bx + L.by + L.bz;
+    const float rn2 = __fmul_rn(rn, rn), rg2 = __fmul_rn(rg, rg);
+    NbrEntry list[kMaxNN];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        const float4 p4 = g.spos[s];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
+        const int gi = g.sidx[s];
+        const float Ip = g.sint[s];
+        const int seg = L.bseg ? (int)(g.skey[s] >> segshift) : 0;
+        const float3 o = g.gmin[seg];
+        float3 nrm = make_float3(0.0f, 0.0f, 0.0f);
+        if (do_normals)
+        {
+            float s1x = 0, s1y = 0, s1z = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
+            int k = 0;
+            if (max_nn <= 0)
+            {
+                grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
+                    if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                    {
+                        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                        s1x += dx, s1y += dy, s1z += dz;
+                        sxx += dx * dx, sxy += dx * dy, sxz += dx * dz;
+                        syy += dy * dy, syz += dy * dz, szz += dz * dz;
+                        ++k;
+                    }
+                });
+            }
+            else
+            {
+                int cnt = 0;
+                grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
+                    const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+                    if (!(d2 < rn2))
+                        return;
+                    const int idx = g.sidx[t];
+                    if (cnt == max_nn)
+                    {
+                        const NbrEntry &w = list[cnt - 1];
+                        if (!(d2 < w.d2 || (d2 == w.d2 && idx < w.idx)))
+                            return;
+                        --cnt;
+                    }
+                    int j = cnt;
+                    while (j > 0 && (list[j - 1].d2 > d2 || (list[j - 1].d2 == d2 && list[j - 1].idx > idx)))
+                    {
+                        list[j] = list[j - 1];
+                        --j;
+                    }
+                    list[j] = NbrEntry{d2, idx, t};
+                    ++cnt;
+                });
+                for (int j = 0; j < cnt; ++j)
+                {
+                    const float4 q = g.spos[list[j].t];
+                    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                    s1x += dx, s1y += dy, s1z += dz;
+                    sxx += dx * dx, sxy += dx * dy, sxz += dx * dz;
+                    syy += dy * dy, syz += dy * dz, szz += dz * dz;
+                }
+                k = cnt;
+            }
+            if (k >= 3)
+            {
+                const float ik = 1.0f / (float)k;
+                const float mx = s1x * ik, my = s1y * ik, mz = s1z * ik;
+                const float c00 = sxx * ik - mx * mx, c01 = sxy * ik - mx * my, c02 = sxz * ik - mx * mz;
+                const float c11 = syy * ik - my * my, c12 = syz * ik - my * mz, c22 = szz * ik - mz * mz;
+                if (!smallest_eigvec_f32(c00, c01, c02, c11, c12, c22, nrm))
+                {
+                    // near-degenerate: rebuild the covariance in FP64 and use Jacobi
+                    double S1[3] = {0, 0, 0}, S2[3][3] = {{0}};
+                    int kk = 0;
+                    auto acc = [&](float4 q) {
+                        const double d[3] = {(double)q.x - (double)p.x, (double)q.y - (double)p.y,
+                                             (double)q.z - (double)p.z};
+                        for (int a = 0; a < 3; ++a)
+                        {
+                            S1[a] += d[a];
+                            for (int b = 0; b < 3; ++b)
+                                S2[a][b] += d[a] * d[b];
+                        }
+                        ++kk;
+                    };
+                    if (max_nn <= 0)
+                        grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
+                            if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                                acc(q);
+                        });
+                    else
+                        for (int j = 0; j < k; ++j)
+                            acc(g.spos[list[j].t]);
+                    double C[3][3], mu[3];
+                    for (int a = 0; a < 3; ++a)
+                        mu[a] = S1[a] / kk;
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b)
+                            C[a][b] = S2[a][b] / kk - mu[a] * mu[b];
+                    double v[3];
+                    jacobi_smallest(C, v);
+                    nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
+                }
+                // orient against (0, 0, -1) (cuda_estimate_normals.cu:131-151)
+                if (nrm.z > 0.0f)
+                    nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+            }
+            if (nrm_out)
+                nrm_out[gi] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
+        }
+        else
+        {
+            const float4 q = in_nrm[gi];
+            nrm = make_float3(q.x, q.y, q.z);
+        }
+        float3 grad = make_float3(0.0f, 0.0f, 0.0f);
+        if (do_grad)
+        {
+            int knn = 0;
+            float A00 = 0, A01 = 0, A02 = 0, A11 = 0, A12 = 0, A22 = 0, b0 = 0, b1 = 0, b2 = 0;
+            grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
+                if (!(dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rg2))
+                    return;
+                ++knn;
+                if (t == s)
+                    return;
+                const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                const float sp = dx * nrm.x + dy * nrm.y + dz * nrm.z;
+                const float vx = dx - sp * nrm.x, vy = dy - sp * nrm.y, vz = dz - sp * nrm.z;
+                const float dI = g.sint[t] - Ip;
+                A00 += vx * vx, A01 += vx * vy, A02 += vx * vz;
+                A11 += vy * vy, A12 += vy * vz, A22 += vz * vz;
+                b0 += vx * dI, b1 += vy * dI, b2 += vz * dI;
+            });
+            if (knn >= 5)
+                grad = solve_gradient_system(A00, A01, A02, A11, A12, A22, b0, b1, b2, nrm,
+                                             (float)((knn - 1) * (knn - 1)));
+            if (grd_out)
+                grd_out[gi] = make_float4(grad.x, grad.y, grad.z, 0.0f);
+        }
+        if (attr0)
+            attr0[s] = make_float4(nrm.x, nrm.y, nrm.z, Ip);
+        if (attr1)
+            attr1[s] = make_float4(grad.x, grad.y, grad.z, 0.0f);
+    }
+}
+
+int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_normals, float normal_radius, int max_nn,
+                  bool do_grad, float grad_radius, const float4 *in_nrm, float4 *attr0, float4 *attr1,
+                  float4 *nrm_out, float4 *grd_out)
+{
+    if (max_nn > kMaxNN)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "normals: max_nn above 64 is not supported");
+    if (do_normals && !(normal_radius > 0.0f && normal_radius <= g.dev.cell))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "normals: radius must be in (0, grid cell]");
+    if (do_grad && !(grad_radius > 0.0f && grad_radius <= g.dev.cell))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gradient: radius must be in (0, grid cell]");
+    if (!do_normals && !in_nrm)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gradient: normals needed");
+    const int gs = std::min(grid_for(g.cap), ctx->num_sms * 8);
+    k_normals_grad<<<gs, 256, 0, ctx->stream>>>(g.dev, b.seg_off + b.P, do_normals ? 1 : 0, normal_radius, max_nn,
+                                                do_grad ? 1 : 0, grad_radius, in_nrm, attr0, attr1, nrm_out, grd_out);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+} // namespace gca3d

@@ -1,0 +1,381 @@
+// schedule.cu -- the coarse-to-fine colored ICP schedule for one or many pairs.
+//
+// reference: color_icp (src/registration/color_icp.hpp:16-63, color_icp.cu:151-234);
+// the coarse-to-fine schedule exists in the reference only as a commented example
+// (apps/test_color_icp.cpp:378-400).
+//
+// Per scale, for all pairs at once: voxel-downsample sources and targets (or copy
+// them when the scale has no voxel size), build one target grid (cell = the
+// largest radius used), estimate target normals and colour gradients in grid
+// order, then launch one fused ICP kernel per iteration.  Nothing on the way
+// synchronises with the host unless the plain mode is chosen, which, like the
+// reference, checks convergence on the host after every iteration.  A plan runs
+// the schedule once to size its scratch memory and then captures it as one CUDA
+// graph that execute replays.
+#include "icp.cuh"
+#include "stages.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <utility>
+
+using namespace gca3d;
+
+namespace gca3d
+{
+int make_segsrc(gca3d_context *ctx, gca3d_cloud *const *clouds, int P, SegSrc **out);
+}
+
+struct gca3d_icp_plan
+{
+    gca3d_context *ctx = nullptr;
+    int P = 0;
+    std::vector<gca3d_cloud *> src, tgt;
+    gca3d_icp_params prm{};
+    Arena arena;
+    SegSrc *d_src = nullptr, *d_tgt = nullptr;
+    PairState *d_state = nullptr;
+    PairState *h_state = nullptr;
+    double *d_Tinit = nullptr, *h_Tinit = nullptr;
+    int max_blocks = 0;
+    int64_t src_cap = 0, tgt_cap = 0, src_max = 0, tgt_max = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t kernels_per_run = 0;
+    bool host_checks = false; // plain mode: convergence test read back after every iteration
+};
+
+namespace
+{
+
+int validate_params(gca3d_context *ctx, const gca3d_icp_params *p)
+{
+    if (!p || p->n_scales < 1 || p->n_scales > GCA3D_MAX_SCALES)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: n_scales must be in [1, 8]");
+    // cuda_color_icp_build_least_square.cu:438-441
+    if (!(p->lambda >= 0.0f && p->lambda <= 1.0f))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: lambda must be in [0, 1]");
+    if (p->update_map != GCA3D_UPDATE_EULER_ZYX && p->update_map != GCA3D_UPDATE_SE3_EXP)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: unknown update map");
+    for (int s = 0; s < p->n_scales; ++s)
+    {
+        const gca3d_scale &S = p->scales[s];
+        if (S.max_iter < 0 || !(S.max_corr > 0.0f) || !(S.grad_radius > 0.0f) || S.max_nn < 0 || S.max_nn > 64)
+            return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: bad scale parameters");
+        const bool need_normals = !(S.voxel <= 0.0f && p->keep_target_normals);
+        if (need_normals && !(S.normal_radius > 0.0f))
+            return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: normal radius must be > 0");
+    }
+    return GCA3D_OK;
+}
+
+int read_states(gca3d_icp_plan *pl)
+{
+    gca3d_context *ctx = pl->ctx;
+    GCA_CUDA(ctx, cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(PairState) * pl->P, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GCA3D_OK;
+}
+
+// enqueue the whole schedule on the context stream (eager or under capture)
+int run_schedule(gca3d_icp_plan *pl, bool capturing)
+{
+    gca3d_context *ctx = pl->ctx;
+    const gca3d_icp_params &p = pl->prm;
+    const int P = pl->P;
+    int st = icp_state_init(ctx, pl->d_state, P, pl->d_Tinit);
+    if (st)
+        return st;
+    for (int si = 0; si < p.n_scales; ++si)
+    {
+        const gca3d_scale &S = p.scales[si];
+        const bool keep = S.voxel <= 0.0f && p.keep_target_normals;
+        Batch bs, bt;
+        if (S.voxel > 0.0f)
+        {
+            if ((st = voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs)))
+                return st;
+            if ((st = voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt)))
+                return st;
+        }
+        else
+        {
+            if ((st = batch_alloc(ctx, bs, P, pl->src_cap, pl->src_max, false, false)))
+                return st;
+            if ((st = gather_stage(ctx, pl->d_src, P, pl->src_max, bs, false)))
+                return st;
+            if ((st = batch_alloc(ctx, bt, P, pl->tgt_cap, pl->tgt_max, keep, false)))
+                return st;
+            if ((st = gather_stage(ctx, pl->d_tgt, P, pl->tgt_max, bt, keep)))
+                return st;
+        }
+        float cell = std::max(S.max_corr, S.grad_radius);
+        if (!keep)
+            cell = std::max(cell, S.normal_radius);
+        Grid g;
+        if ((st = grid_build(ctx, bt, cell, kOriginPadF32, nullptr, g)))
+            return st;
+        float4 *attr0 = ctx->arena.get<float4>(g.cap);
+        float4 *attr1 = ctx->arena.get<float4>(g.cap);
+        double *partials = ctx->arena.get<double>((size_t)std::max(pl->max_blocks, 1) * kTermsPad);
+        int *bmap = ctx->arena.get<int>(P + 1);
+        if (!attr0 || !attr1 || !partials || !bmap)
+            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
+        if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
+                                keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
+            return st;
+        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, si == 0)))
+            return st;
+        IcpScale prm;
+        prm.max_corr = S.max_corr;
+        prm.sqrt_lg = sqrtf(p.lambda);
+        prm.sqrt_lc = sqrtf(1.0f - p.lambda);
+        prm.update_map = p.update_map;
+        prm.rot_eps = p.rot_eps;
+        prm.trans_eps = p.trans_eps;
+        for (int it = 0; it < S.max_iter; ++it)
+        {
+            if ((st = icp_iteration(ctx, bs, g, attr0, attr1, pl->d_state, bmap, pl->max_blocks, partials, prm,
+                                    p.compensated != 0, nullptr)))
+                return st;
+            if (pl->host_checks && !capturing)
+            {
+                // the reference's control flow: the step is inspected on the host
+                if ((st = read_states(pl)))
+                    return st;
+                bool any = false;
+                for (int k = 0; k < P; ++k)
+                    any |= pl->h_state[k].active != 0;
+                if (!any)
+                    break;
+            }
+        }
+    }
+    return GCA3D_OK;
+}
+
+int run_with_arena(gca3d_icp_plan *pl, bool capturing)
+{
+    pl->ctx->arena.swap(pl->arena);
+    pl->ctx->arena.reset();
+    const int64_t l0 = pl->ctx->launches;
+    int st = run_schedule(pl, capturing);
+    if (!st && pl->ctx->arena.failed)
+        st = fail(pl->ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp plan: scratch memory");
+    pl->kernels_per_run = pl->ctx->launches - l0;
+    pl->ctx->arena.swap(pl->arena);
+    return st;
+}
+
+void fill_results(const gca3d_icp_plan *pl, gca3d_icp_result *res)
+{
+    for (int k = 0; k < pl->P; ++k)
+    {
+        const PairState &S = pl->h_state[k];
+        gca3d_icp_result &r = res[k];
+        memcpy(r.T, S.T, sizeof r.T);
+        r.rmse_ref = S.rmse_ref;
+        r.fitness = S.fitness;
+        r.inlier_rmse = S.inlier_rmse;
+        r.iterations = S.iters;
+        r.converged = S.converged;
+        r.status = S.status;
+        r.n_src = S.nsrc;
+        r.n_tgt = S.ntgt;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
+{
+    if (!pl)
+        return GCA3D_ERR_INVALID_VALUE;
+    if (pl->ctx)
+        cudaStreamSynchronize(pl->ctx->stream);
+    if (pl->exec)
+        cudaGraphExecDestroy(pl->exec);
+    if (pl->graph)
+        cudaGraphDestroy(pl->graph);
+    cudaFree(pl->d_src);
+    cudaFree(pl->d_tgt);
+    cudaFree(pl->d_state);
+    cudaFree(pl->d_Tinit);
+    if (pl->h_state)
+        cudaFreeHost(pl->h_state);
+    if (pl->h_Tinit)
+        cudaFreeHost(pl->h_Tinit);
+    pl->arena.release();
+    delete pl;
+    return GCA3D_OK;
+}
+
+static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
+                       const gca3d_icp_params *params, bool capture, gca3d_icp_plan **out)
+{
+    if (!ctx || !out || P < 1 || P > kMaxSegments || !src || !tgt)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: bad arguments (1 <= pairs <= 4096)");
+    *out = nullptr;
+    int st = validate_params(ctx, params);
+    if (st)
+        return st;
+    for (int k = 0; k < P; ++k)
+    {
+        if (!src[k] || !tgt[k])
+            return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: null cloud");
+        if (params->keep_target_normals && params->scales[0].voxel <= 0.0f && !tgt[k]->has_normals)
+            return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: the target has no normals (estimate normals first)");
+    }
+    auto *pl = new gca3d_icp_plan();
+    pl->ctx = ctx;
+    pl->P = P;
+    pl->src.assign(src, src + P);
+    pl->tgt.assign(tgt, tgt + P);
+    pl->prm = *params;
+    pl->host_checks = !params->use_graph;
+    int nb = 0;
+    for (int k = 0; k < P; ++k)
+    {
+        pl->src_cap += src[k]->capacity;
+        pl->tgt_cap += tgt[k]->capacity;
+        pl->src_max = std::max(pl->src_max, src[k]->capacity);
+        pl->tgt_max = std::max(pl->tgt_max, tgt[k]->capacity);
+        nb += div_up(src[k]->capacity, kIcpChunk);
+    }
+    pl->max_blocks = std::max(nb, 1);
+    // device tables and state live outside the scratch arena
+    std::vector<SegSrc> hs(P), ht(P);
+    for (int k = 0; k < P; ++k)
+    {
+        hs[k] = SegSrc{src[k]->pos, src[k]->col, nullptr, src[k]->d_count};
+        ht[k] = SegSrc{tgt[k]->pos, tgt[k]->col, tgt[k]->has_normals ? tgt[k]->nrm : nullptr, tgt[k]->d_count};
+    }
+    if (cudaMalloc(&pl->d_src, sizeof(SegSrc) * P) != cudaSuccess ||
+        cudaMalloc(&pl->d_tgt, sizeof(SegSrc) * P) != cudaSuccess ||
+        cudaMalloc(&pl->d_state, sizeof(PairState) * P) != cudaSuccess ||
+        cudaMalloc(&pl->d_Tinit, sizeof(double) * 16 * P) != cudaSuccess ||
+        cudaMallocHost(&pl->h_state, sizeof(PairState) * P) != cudaSuccess ||
+        cudaMallocHost(&pl->h_Tinit, sizeof(double) * 16 * P) != cudaSuccess)
+    {
+        cudaGetLastError();
+        gca3d_icp_plan_destroy(pl);
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp plan: allocation");
+    }
+    cudaMemcpy(pl->d_src, hs.data(), sizeof(SegSrc) * P, cudaMemcpyHostToDevice);
+    cudaMemcpy(pl->d_tgt, ht.data(), sizeof(SegSrc) * P, cudaMemcpyHostToDevice);
+    for (int k = 0; k < P; ++k)
+        for (int j = 0; j < 16; ++j)
+            pl->h_Tinit[16 * k + j] = (j % 5 == 0) ? 1.0 : 0.0;
+    cudaMemcpy(pl->d_Tinit, pl->h_Tinit, sizeof(double) * 16 * P, cudaMemcpyHostToDevice);
+    if (capture)
+    {
+        // size the scratch with one eager run, then capture the identical sequence
+        st = run_with_arena(pl, false);
+        if (!st)
+        {
+            cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            st = e != cudaSuccess ? cuda_fail(ctx, e, "icp plan warm-up") : consume_device_error(ctx, "icp plan");
+        }
+        if (!st)
+        {
+            pl->arena.frozen = true;
+            cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess)
+                st = cuda_fail(ctx, e, "cudaStreamBeginCapture");
+            else
+            {
+                int st2 = run_with_arena(pl, true);
+                cudaGraph_t g = nullptr;
+                e = cudaStreamEndCapture(ctx->stream, &g);
+                pl->graph = g;
+                if (st2)
+                    st = st2;
+                else if (e != cudaSuccess)
+                    st = cuda_fail(ctx, e, "cudaStreamEndCapture");
+                else
+                {
+                    e = cudaGraphInstantiate(&pl->exec, pl->graph, 0);
+                    if (e != cudaSuccess)
+                        st = cuda_fail(ctx, e, "cudaGraphInstantiate");
+                }
+            }
+            pl->arena.frozen = false;
+        }
+        if (st)
+        {
+            cudaGetLastError();
+            gca3d_icp_plan_destroy(pl);
+            return st;
+        }
+    }
+    *out = pl;
+    return GCA3D_OK;
+}
+
+int gca3d_icp_plan_create(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
+                          const gca3d_icp_params *params, gca3d_icp_plan **plan)
+{
+    return plan_create(ctx, n_pairs, src, tgt, params, params && params->use_graph, plan);
+}
+
+int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_result *results)
+{
+    if (!pl)
+        return GCA3D_ERR_INVALID_VALUE;
+    gca3d_context *ctx = pl->ctx;
+    for (int k = 0; k < pl->P; ++k)
+        for (int j = 0; j < 16; ++j)
+            pl->h_Tinit[16 * k + j] = T_init ? T_init[16 * k + j] : ((j % 5 == 0) ? 1.0 : 0.0);
+    GCA_CUDA(ctx, cudaMemcpyAsync(pl->d_Tinit, pl->h_Tinit, sizeof(double) * 16 * pl->P, cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    int st;
+    if (pl->exec)
+    {
+        GCA_CUDA(ctx, cudaGraphLaunch(pl->exec, ctx->stream));
+        ctx->launches += pl->kernels_per_run;
+    }
+    else if ((st = run_with_arena(pl, false)))
+        return st;
+    if (!results)
+        return GCA3D_OK;
+    if ((st = read_states(pl)))
+        return st;
+    if ((st = consume_device_error(ctx, "icp")))
+        return st;
+    fill_results(pl, results);
+    return GCA3D_OK;
+}
+
+int gca3d_icp_plan_kernels(gca3d_icp_plan *pl, int64_t *n)
+{
+    if (!pl || !n)
+        return GCA3D_ERR_INVALID_VALUE;
+    *n = pl->kernels_per_run;
+    return GCA3D_OK;
+}
+
+int gca3d_color_icp_batched(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
+                            const gca3d_icp_params *params, const double *T_init, gca3d_icp_result *results)
+{
+    if (!results)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: results needed");
+    gca3d_icp_plan *pl = nullptr;
+    int st = plan_create(ctx, n_pairs, src, tgt, params, false, &pl);
+    if (st)
+        return st;
+    st = gca3d_icp_plan_execute(pl, T_init, results);
+    gca3d_icp_plan_destroy(pl);
+    return st;
+}
+
+int gca3d_color_icp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt, const gca3d_icp_params *params,
+                    const double T_init[16], gca3d_icp_result *result)
+{
+    return gca3d_color_icp_batched(ctx, 1, &src, &tgt, params, T_init, result);
+}
+
+} // extern "C"

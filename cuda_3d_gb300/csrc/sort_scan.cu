@@ -1,0 +1,440 @@
+// sort_scan.cu -- LSD radix sort of (uint64 key, int32 value) pairs and a device-wide
+// exclusive scan, both single-pass per digit / per scan with decoupled look-back.
+//
+// The sort replaces the reference's thrust::sort_by_key calls
+// (src/geometry/cuda_voxel_grid_down_sample.cu:136, src/geometry/cuda_nn_search.cu:581-582):
+// it is stable, so equal keys keep ascending input (original index) order, which is
+// the order the voxel sums and the neighbour scans are defined in.
+//
+// Every look-back wait is bounded: after kSpinLimit polls the kernel records
+// kErrTimeout in the context's error word and continues, so a scheduling fault
+// shows up as a status, never as a hung GPU.
+#include "internal.cuh"
+
+namespace gca3d
+{
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems; // 2048 keys per tile
+constexpr int kSortWarps = kSortThreads / 32;
+
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kFlagMask = 3u << 30;
+constexpr uint32_t kCountMask = (1u << 30) - 1;
+
+struct SortCtl
+{
+    uint32_t hist[8][256];
+    uint32_t off[8][256];
+    int trivial[8];
+    int in_sel[8];
+    uint32_t tile_ctr[8];
+};
+
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// histogram of all 8 byte-digits; also clears the first look-back status buffer
+__global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *d_n, SortCtl *ctl,
+                            uint32_t *status0, int64_t status_words)
+{
+    __shared__ uint32_t h[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
+        (&h[0][0])[i] = 0;
+    __syncthreads();
+    const int n = *d_n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    {
+        uint64_t k = keys[i];
+#pragma unroll
+        for (int d = 0; d < 8; ++d)
+            atomicAdd(&h[d][(k >> (8 * d)) & 255], 1u);
+    }
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < status_words;
+         i += (int64_t)gridDim.x * blockDim.x)
+        status0[i] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
+    {
+        uint32_t c = (&h[0][0])[i];
+        if (c)
+            atomicAdd(&(&ctl->hist[0][0])[i], c);
+    }
+}
+
+// bucket offsets per digit, trivial-pass detection and ping-pong bookkeeping
+__global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *d_sel)
+{
+    __shared__ uint32_t s[256];
+    __shared__ int triv;
+    const int n = *d_n;
+    const int t = threadIdx.x;
+    for (int d = 0; d < npasses; ++d)
+    {
+        if (t == 0)
+            triv = 0;
+        uint32_t c = ctl->hist[d][t];
+        s[t] = c;
+        __syncthreads();
+        if ((int)c == n)
+            triv = 1;
+        // inclusive Hillis-Steele scan over 256 digits
+        for (int o = 1; o < 256; o <<= 1)
+        {
+            uint32_t v = t >= o ? s[t - o] : 0;
+            __syncthreads();
+            s[t] += v;
+            __syncthreads();
+        }
+        ctl->off[d][t] = s[t] - c;
+        if (t == 0)
+            ctl->trivial[d] = triv || n <= 1;
+        __syncthreads();
+    }
+    if (t == 0)
+    {
+        int sel = 0;
+        for (int d = 0; d < npasses; ++d)
+        {
+            ctl->in_sel[d] = sel;
+            if (!ctl->trivial[d])
+                sel ^= 1;
+        }
+        *d_sel = sel;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_sort_pass(
+    uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, uint32_t *status,
+    uint32_t *status_next, int64_t status_words, int pass, const int32_t *d_n, int *d_err)
+{
+    __shared__ uint32_t s_whist[kSortWarps][256];
+    __shared__ uint32_t s_excl[256];
+    __shared__ uint32_t s_gbase[256];
+    __shared__ uint64_t s_keys[kSortTile];
+    __shared__ int32_t s_vals[kSortTile];
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_wsum[kSortWarps];
+
+    // clear the status buffer of the next pass (the one of the previous pass is done)
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < status_words;
+         i += (int64_t)gridDim.x * blockDim.x)
+        status_next[i] = 0;
+    if (ctl->trivial[pass])
+        return;
+    const int n = *d_n;
+    const int ntiles = (n + kSortTile - 1) / kSortTile;
+    if (threadIdx.x == 0)
+        s_tile = atomicAdd(&ctl->tile_ctr[pass], 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if ((int)tile >= ntiles)
+        return;
+    const int sel = ctl->in_sel[pass];
+    const uint64_t *kin = sel ? keys1 : keys0;
+    const int32_t *vin = sel ? vals1 : vals0;
+    uint64_t *kout = sel ? keys0 : keys1;
+    int32_t *vout = sel ? vals0 : vals1;
+    const int shift = pass * 8;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+
+    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads)
+        (&s_whist[0][0])[i] = 0;
+    __syncthreads();
+
+    uint64_t k[kSortItems];
+    int32_t v[kSortItems];
+    uint32_t dig[kSortItems], rank[kSortItems];
+    const int64_t base = (int64_t)tile * kSortTile + warp * 32 * kSortItems;
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        int64_t idx = base + it * 32 + lane;
+        if (idx < n)
+        {
+            k[it] = kin[idx];
+            v[it] = vin[idx];
+            dig[it] = (uint32_t)(k[it] >> shift) & 255u;
+        }
+        else
+        {
+            k[it] = 0;
+            v[it] = 0;
+            dig[it] = 256u;
+        }
+    }
+    // warp-level stable ranking (match peers with the same digit)
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        unsigned peers = __match_any_sync(0xffffffffu, dig[it]);
+        int leader = __ffs(peers) - 1;
+        uint32_t b = 0;
+        if (lane == leader && dig[it] < 256u)
+        {
+            b = s_whist[warp][dig[it]];
+            s_whist[warp][dig[it]] = b + __popc(peers);
+        }
+        b = __shfl_sync(0xffffffffu, b, leader);
+        rank[it] = b + __popc(peers & lt_mask);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: prefix over warps, tile total
+    const int t = threadIdx.x;
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w)
+    {
+        uint32_t c = s_whist[w][t];
+        s_whist[w][t] = tot;
+        tot += c;
+    }
+    // decoupled look-back across tiles for digit t
+    uint32_t excl = 0;
+    uint32_t *st = status + (int64_t)tile * 256 + t;
+    if (tile == 0)
+    {
+        st_release(st, kFlagInc | tot);
+    }
+    else
+    {
+        st_release(st, kFlagAgg | tot);
+        int64_t p = (int64_t)tile - 1;
+        while (p >= 0)
+        {
+            const uint32_t *ps = status + p * 256 + t;
+            uint32_t s = ld_acquire(ps);
+            uint32_t spins = 0;
+            while ((s & kFlagMask) == 0)
+            {
+                if (++spins > kSpinLimit)
+                {
+                    atomicOr(d_err, kErrTimeout);
+                    break;
+                }
+                if (spins > 64)
+                    __nanosleep(64);
+                s = ld_acquire(ps);
+            }
+            excl += s & kCountMask;
+            if ((s & kFlagMask) != kFlagAgg)
+                break;
+            --p;
+        }
+        st_release(st, kFlagInc | (excl + tot));
+    }
+    // exclusive scan of the tile totals over digits (block scan of 256 values)
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int w = 0; w < warp; ++w)
+        wpre += s_wsum[w];
+    const uint32_t tile_excl = wpre + x - tot;
+    s_excl[t] = tile_excl;
+    s_gbase[t] = ctl->off[pass][t] + excl - tile_excl;
+    __syncthreads();
+    // stage in tile-sorted order
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        if (dig[it] < 256u)
+        {
+            uint32_t pl = s_excl[dig[it]] + s_whist[warp][dig[it]] + rank[it];
+            s_keys[pl] = k[it];
+            s_vals[pl] = v[it];
+        }
+    }
+    __syncthreads();
+    const int cnt = min(kSortTile, n - (int)tile * kSortTile);
+    for (int j = threadIdx.x; j < cnt; j += kSortThreads)
+    {
+        uint64_t kk = s_keys[j];
+        uint32_t d = (uint32_t)(kk >> shift) & 255u;
+        uint32_t g = s_gbase[d] + j;
+        kout[g] = kk;
+        vout[g] = s_vals[j];
+    }
+}
+
+int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t cap, int max_bits,
+               const int * /*d_key_bits*/)
+{
+    const int npasses = max_bits <= 0 ? 1 : (max_bits + 7) / 8;
+    const int64_t ntiles = (cap + kSortTile - 1) / kSortTile;
+    const int64_t status_words = (ntiles > 0 ? ntiles : 1) * 256;
+    SortCtl *ctl = ctx->arena.get<SortCtl>(1);
+    uint32_t *status = ctx->arena.get<uint32_t>(2 * status_words);
+    if (!ctl || !status || !sb.d_sel)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "radix_sort: scratch");
+    GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(SortCtl), ctx->stream));
+    int hist_grid = (int)std::min<int64_t>(grid_for(cap, kBlock * 8), (int64_t)ctx->num_sms * 8);
+    k_sort_hist<<<hist_grid, kBlock, 0, ctx->stream>>>(sb.keys[0], d_n, ctl, status, status_words);
+    GCA_CHECK_LAUNCH(ctx);
+    k_sort_prep<<<1, 256, 0, ctx->stream>>>(ctl, d_n, npasses, sb.d_sel);
+    GCA_CHECK_LAUNCH(ctx);
+    for (int p = 0; p < npasses; ++p)
+    {
+        k_sort_pass<<<(int)(ntiles > 0 ? ntiles : 1), kSortThreads, 0, ctx->stream>>>(
+            sb.keys[0], sb.vals[0], sb.keys[1], sb.vals[1], ctl, status + (p & 1) * status_words,
+            status + ((p + 1) & 1) * status_words, status_words, p, d_n, ctx->d_err);
+        GCA_CHECK_LAUNCH(ctx);
+    }
+    return GCA3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan (int32), single pass with decoupled look-back
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr unsigned long long kSFlagAgg = 1ull << 62;
+constexpr unsigned long long kSFlagInc = 2ull << 62;
+constexpr unsigned long long kSFlagMask = 3ull << 62;
+constexpr unsigned long long kSValMask = (1ull << 62) - 1;
+
+struct ScanCtl
+{
+    uint32_t tile_ctr;
+};
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict__ in, int32_t *out,
+                                                       const int32_t *d_n, ScanCtl *ctl,
+                                                       unsigned long long *status, int32_t *d_total,
+                                                       int *d_err)
+{
+    __shared__ uint32_t s_tile;
+    __shared__ long long s_wsum[kScanThreads / 32];
+    __shared__ long long s_prefix;
+    const int n = *d_n;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    if (threadIdx.x == 0)
+        s_tile = atomicAdd(&ctl->tile_ctr, 1u);
+    __syncthreads();
+    const int tile = (int)s_tile;
+    if (tile >= ntiles)
+    {
+        if (tile == 0 && threadIdx.x == 0 && d_total)
+            *d_total = 0; // empty input
+        return;
+    }
+    const int64_t base = (int64_t)tile * kScanTile + threadIdx.x * kScanItems;
+    long long v[kScanItems];
+    long long tsum = 0;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i)
+    {
+        v[i] = base + i < n ? (long long)in[base + i] : 0;
+        tsum += v[i];
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    long long x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_wsum[warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        long long agg = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w)
+            agg += s_wsum[w];
+        unsigned long long *st = status + tile;
+        long long excl = 0;
+        if (tile == 0)
+            st_release64(st, kSFlagInc | (unsigned long long)agg);
+        else
+        {
+            st_release64(st, kSFlagAgg | (unsigned long long)agg);
+            for (int p = tile - 1; p >= 0; --p)
+            {
+                unsigned long long s = ld_acquire64(status + p);
+                uint32_t spins = 0;
+                while ((s & kSFlagMask) == 0)
+                {
+                    if (++spins > kSpinLimit)
+                    {
+                        atomicOr(d_err, kErrTimeout);
+                        break;
+                    }
+                    if (spins > 64)
+                        __nanosleep(64);
+                    s = ld_acquire64(status + p);
+                }
+                excl += (long long)(s & kSValMask);
+                if ((s & kSFlagMask) != kSFlagAgg)
+                    break;
+            }
+            st_release64(st, kSFlagInc | (unsigned long long)(excl + agg));
+        }
+        s_prefix = excl;
+        if (tile == ntiles - 1 && d_total)
+            *d_total = (int32_t)(excl + agg);
+    }
+    __syncthreads();
+    long long run = s_prefix;
+    for (int w = 0; w < warp; ++w)
+        run += s_wsum[w];
+    run += x - tsum;
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i)
+    {
+        if (base + i < n)
+            out[base + i] = (int32_t)run;
+        run += v[i];
+    }
+}
+
+int exclusive_scan(gca3d_context *ctx, const int32_t *in, int32_t *out, const int32_t *d_n,
+                   int64_t cap, int32_t *d_total)
+{
+    const int64_t ntiles = (cap + kScanTile - 1) / kScanTile;
+    ScanCtl *ctl = ctx->arena.get<ScanCtl>(1);
+    unsigned long long *status = ctx->arena.get<unsigned long long>(ntiles > 0 ? ntiles : 1);
+    if (!ctl || !status)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "exclusive_scan: scratch");
+    GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(ScanCtl), ctx->stream));
+    GCA_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(unsigned long long) * (ntiles > 0 ? ntiles : 1), ctx->stream));
+    k_scan<<<(int)(ntiles > 0 ? ntiles : 1), kScanThreads, 0, ctx->stream>>>(in, out, d_n, ctl, status, d_total,
+                                                                             ctx->d_err);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+} // namespace gca3d

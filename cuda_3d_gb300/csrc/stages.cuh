@@ -1,0 +1,81 @@
+// stages.cuh -- batched stage interfaces shared by the translation units.
+#pragma once
+
+#include "internal.cuh"
+
+namespace gca3d
+{
+
+struct Pose34f
+{
+    float m[12]; // row-major 3x4
+};
+Pose34f pose_to_f32(const double T[16]);
+
+// P point sets back to back in structure-of-arrays form
+struct Batch
+{
+    float4 *pos = nullptr, *col = nullptr, *nrm = nullptr, *grd = nullptr;
+    int32_t *seg_off = nullptr; // device [P + 1]
+    int P = 0;
+    int64_t cap = 0;         // total capacity
+    int64_t max_seg_cap = 0; // largest segment capacity
+};
+
+// a source cloud of a batched stage, read through a device pointer table
+struct SegSrc
+{
+    const float4 *pos;
+    const float4 *col;
+    const float4 *nrm;
+    const int32_t *d_n;
+};
+
+enum GridOrigin : int
+{
+    kOriginPadF32 = 0, // aabb_min - 1.5f * cell            (color_icp.cu:55-66, point_cloud.cu:519-537)
+    kOriginPadF64 = 1, // (float)((double)aabb_min - 1.5 * (double)cell)   (point_cloud.cu:153-159)
+    kOriginGiven = 2,  // caller-supplied origin (single segment)
+};
+
+struct Grid
+{
+    GridDev dev;
+    int64_t cap = 0;
+    int P = 0;
+    uint32_t hcap = 0;
+};
+
+int seg_bounds(gca3d_context *ctx, const float4 *pos, const int32_t *seg_off, int P, int64_t max_seg_cap,
+               int *ord);
+int single_seg_offsets(gca3d_context *ctx, const int32_t *d_n, int32_t *seg_off);
+
+// allocate a batch from the context arena
+int batch_alloc(gca3d_context *ctx, Batch &b, int P, int64_t cap, int64_t max_seg_cap, bool nrm, bool grd);
+
+// stage 0 of a scale: voxel downsample (voxel > 0) or gather copy into a batch
+int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap, int64_t max_seg_cap,
+                float voxel, Batch &out);
+int gather_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t max_seg_cap, Batch &out,
+                 bool with_normals);
+
+// uniform grid over a batch; cell edge `cell`
+int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, const float *host_origin,
+               Grid &g);
+
+// fused normals + colour gradient over the grid's own points (targets).  Writes
+// attr0 = {n, intensity} and attr1 = {gradient, 0} in grid order, and scatters
+// normals / gradients back to the batch (original order) when nrm_out / grd_out
+// are set.  in_nrm (original order) supplies normals when do_normals is false.
+int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_normals, float normal_radius,
+                  int max_nn, bool do_grad, float grad_radius, const float4 *in_nrm, float4 *attr0,
+                  float4 *attr1, float4 *nrm_out, float4 *grd_out);
+
+// nearest neighbour / radius lists of query batch points against a single-segment grid
+int nn_query(gca3d_context *ctx, const float4 *qpos, const int32_t *d_nq, int64_t qcap, const Grid &g,
+             float radius, int32_t *out_idx);
+int radius_query(gca3d_context *ctx, const float4 *qpos, const int32_t *d_nq, int64_t qcap, const Grid &g,
+                 float radius, int32_t *counts, int32_t *starts, int32_t *list, int64_t list_cap,
+                 int32_t *d_total);
+
+} // namespace gca3d

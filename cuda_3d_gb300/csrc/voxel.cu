@@ -1,0 +1,338 @@
+// voxel.cu -- batched voxel-grid downsampling.
+//
+// reference: cuda_voxel_grid_downsample (src/geometry/cuda_voxel_grid_down_sample.cu:123-161)
+// and point_cloud::voxel_grid_down_sample (src/geometry/point_cloud.cu:198-229).
+//
+// Per segment (cloud) the key is floor((p - aabb_min) / v) per axis, as the
+// reference computes it.  The three axis keys of every segment are packed, with the
+// segment index above them, into one 64-bit key whose numeric order is the
+// reference's lexicographic (kx, ky, kz) order; one stable radix sort then orders
+// all segments at once.  A voxel's sum runs sequentially over its points in
+// ascending original index (the sort is stable), so the downsampled set is
+// bit-exact against the oracle; the mean is xyz / n and rgb * (1 / n) as in
+// src/geometry/type.hpp:58-62.
+#include "stages.cuh"
+
+#include <algorithm>
+
+namespace gca3d
+{
+
+int batch_alloc(gca3d_context *ctx, Batch &b, int P, int64_t cap, int64_t max_seg_cap, bool nrm, bool grd)
+{
+    Arena &A = ctx->arena;
+    b.P = P;
+    b.cap = cap;
+    b.max_seg_cap = max_seg_cap;
+    int64_t c = std::max<int64_t>(cap, 1);
+    b.pos = A.get<float4>(c);
+    b.col = A.get<float4>(c);
+    b.nrm = nrm ? A.get<float4>(c) : nullptr;
+    b.grd = grd ? A.get<float4>(c) : nullptr;
+    b.seg_off = A.get<int32_t>(P + 1);
+    if (!b.pos || !b.col || (nrm && !b.nrm) || (grd && !b.grd) || !b.seg_off)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "batch_alloc: scratch");
+    return GCA3D_OK;
+}
+
+// exclusive prefix of the segment sizes (one block)
+__global__ void k_src_prefix(const SegSrc *src, int P, int32_t *off)
+{
+    __shared__ int32_t s_base;
+    if (threadIdx.x == 0)
+        s_base = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < P; c0 += blockDim.x)
+    {
+        int i = c0 + threadIdx.x;
+        int v = i < P ? *src[i].d_n : 0;
+        // block inclusive scan (Hillis-Steele over 256)
+        __shared__ int32_t s[256];
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 256; o <<= 1)
+        {
+            int32_t y = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+            __syncthreads();
+            s[threadIdx.x] += y;
+            __syncthreads();
+        }
+        if (i < P)
+            off[i] = s_base + s[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 255)
+            s_base += s[255];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        off[P] = s_base;
+}
+
+__global__ void k_src_bounds_init(int *ord, int P)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * P)
+        ord[i] = (i % 6) < 3 ? float_to_ordered(3.402823466e38f) : float_to_ordered(-3.402823466e38f);
+}
+
+__global__ void k_src_bounds(const SegSrc *src, int *ord)
+{
+    const int seg = blockIdx.y;
+    const int n = *src[seg].d_n;
+    const float4 *pos = src[seg].pos;
+    float mn[3] = {3.402823466e38f, 3.402823466e38f, 3.402823466e38f};
+    float mx[3] = {-3.402823466e38f, -3.402823466e38f, -3.402823466e38f};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        float4 p = pos[i];
+        mn[0] = fminf(mn[0], p.x), mn[1] = fminf(mn[1], p.y), mn[2] = fminf(mn[2], p.z);
+        mx[0] = fmaxf(mx[0], p.x), mx[1] = fmaxf(mx[1], p.y), mx[2] = fmaxf(mx[2], p.z);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+    if ((threadIdx.x & 31) == 0 && n > 0)
+        for (int a = 0; a < 3; ++a)
+        {
+            atomicMin(ord + 6 * seg + a, float_to_ordered(mn[a]));
+            atomicMax(ord + 6 * seg + 3 + a, float_to_ordered(mx[a]));
+        }
+}
+
+// key layout shared by all segments; per-segment origin = unpadded aabb min
+__global__ void k_voxel_layout(const int *ord, int P, float voxel, float3 *origin, KeyLayout *lay, int *d_err)
+{
+    __shared__ uint32_t s_max[3];
+    if (threadIdx.x < 3)
+        s_max[threadIdx.x] = 0;
+    __syncthreads();
+    for (int s = threadIdx.x; s < P; s += blockDim.x)
+    {
+        float mn[3], mx[3];
+        for (int a = 0; a < 3; ++a)
+        {
+            mn[a] = ordered_to_float(ord[6 * s + a]);
+            mx[a] = ordered_to_float(ord[6 * s + 3 + a]);
+        }
+        origin[s] = make_float3(mn[0], mn[1], mn[2]);
+        if (!(mx[0] >= mn[0])) // empty segment
+            continue;
+        for (int a = 0; a < 3; ++a)
+        {
+            int k = cell_of(mx[a], mn[a], voxel);
+            if (k < 0 || k >= (1 << 21))
+            {
+                atomicOr(d_err, kErrKeyBits);
+                k = (1 << 21) - 1;
+            }
+            atomicMax(&s_max[a], (uint32_t)k);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        KeyLayout L;
+        L.bseg = bitlen_u32((uint32_t)(P - 1));
+        L.bx = max(1, bitlen_u32(s_max[0]));
+        L.by = max(1, bitlen_u32(s_max[1]));
+        L.bz = max(1, bitlen_u32(s_max[2]));
+        L.total_bits = L.bseg + L.bx + L.by + L.bz;
+        if (L.total_bits > 64)
+            atomicOr(d_err, kErrKeyBits);
+        *lay = L;
+    }
+}
+
+__global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3 *origin, const KeyLayout *lay,
+                             float voxel, uint64_t *keys, int32_t *vals)
+{
+    const int seg = blockIdx.y;
+    const int n = *src[seg].d_n;
+    const int base = off[seg];
+    const KeyLayout L = *lay;
+    const float3 o = origin[seg];
+    const float4 *pos = src[seg].pos;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        float4 p = pos[i];
+        uint64_t kx = (uint32_t)cell_of(p.x, o.x, voxel), ky = (uint32_t)cell_of(p.y, o.y, voxel),
+                 kz = (uint32_t)cell_of(p.z, o.z, voxel);
+        uint64_t key = ((uint64_t)seg << (L.bx + L.by + L.bz)) | (kx << (L.by + L.bz)) | (ky << L.bz) | kz;
+        keys[base + i] = key;
+        vals[base + i] = base + i;
+    }
+}
+
+__global__ void k_run_flags(SortBuffers sb, const int32_t *d_n, int32_t *flags)
+{
+    const uint64_t *keys = sb.keys[*sb.d_sel];
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_run_starts(const int32_t *flags, const int32_t *vid, const int32_t *d_n, const int32_t *d_m,
+                             int32_t *starts)
+{
+    const int n = *d_n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (flags[i])
+            starts[vid[i]] = i;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        starts[*d_m] = n;
+}
+
+__global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuffers sb, const int32_t *starts,
+                               const int32_t *d_m, const KeyLayout *lay, float4 *opos, float4 *ocol,
+                               int32_t *seg_count)
+{
+    const int m = *d_m;
+    const uint64_t *keys = sb.keys[*sb.d_sel];
+    const int32_t *vals = sb.vals[*sb.d_sel];
+    const KeyLayout L = *lay;
+    const int segshift = L.bx + L.by + L.bz;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m; v += gridDim.x * blockDim.x)
+    {
+        const int s = starts[v], e = starts[v + 1];
+        const int seg = L.bseg ? (int)(keys[s] >> segshift) : 0;
+        const int base = in_off[seg];
+        const float4 *ps = src[seg].pos;
+        const float4 *cs = src[seg].col;
+        int g = vals[s] - base;
+        float4 p = ps[g], c = cs[g];
+        float sx = p.x, sy = p.y, sz = p.z, cr = c.x, cg = c.y, cb = c.z;
+        for (int j = s + 1; j < e; ++j)
+        {
+            g = vals[j] - base;
+            p = ps[g];
+            c = cs[g];
+            sx = __fadd_rn(sx, p.x);
+            sy = __fadd_rn(sy, p.y);
+            sz = __fadd_rn(sz, p.z);
+            cr = __fadd_rn(cr, c.x);
+            cg = __fadd_rn(cg, c.y);
+            cb = __fadd_rn(cb, c.z);
+        }
+        const float fn = (float)(e - s);
+        const float inv = __fdiv_rn(1.0f, fn);
+        const float r = __fmul_rn(cr, inv), gg = __fmul_rn(cg, inv), b = __fmul_rn(cb, inv);
+        opos[v] = make_float4(__fdiv_rn(sx, fn), __fdiv_rn(sy, fn), __fdiv_rn(sz, fn), intensity_of(r, gg, b));
+        ocol[v] = make_float4(r, gg, b, 0.0f);
+        atomicAdd(seg_count + seg, 1);
+    }
+}
+
+// offsets from per-segment counts (one block)
+__global__ void k_counts_to_offsets(const int32_t *count, int P, int32_t *off)
+{
+    if (threadIdx.x == 0)
+    {
+        int32_t s = 0;
+        for (int i = 0; i < P; ++i)
+        {
+            off[i] = s;
+            s += count[i];
+        }
+        off[P] = s;
+    }
+}
+
+int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap, int64_t max_seg_cap,
+                float voxel, Batch &out)
+{
+    if (!(voxel > 0.0f))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "voxel size must be > 0");
+    Arena &A = ctx->arena;
+    const int64_t cap = std::max<int64_t>(total_cap, 1);
+    int32_t *in_off = A.get<int32_t>(P + 1);
+    int *ord = A.get<int>(6 * P);
+    float3 *origin = A.get<float3>(P);
+    KeyLayout *lay = A.get<KeyLayout>(1);
+    SortBuffers sb;
+    sb.keys[0] = A.get<uint64_t>(cap);
+    sb.keys[1] = A.get<uint64_t>(cap);
+    sb.vals[0] = A.get<int32_t>(cap);
+    sb.vals[1] = A.get<int32_t>(cap);
+    sb.d_sel = A.get<int>(1);
+    int32_t *flags = A.get<int32_t>(cap);
+    int32_t *vid = A.get<int32_t>(cap);
+    int32_t *starts = A.get<int32_t>(cap + 1);
+    int32_t *d_m = A.get<int32_t>(1);
+    int32_t *seg_count = A.get<int32_t>(P);
+    if (!in_off || !ord || !origin || !lay || !sb.keys[1] || !sb.vals[1] || !sb.d_sel || !flags ||
+        !vid || !starts || !d_m || !seg_count)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "voxel_stage: scratch");
+    if (!out.pos)
+    {
+        int st = batch_alloc(ctx, out, P, total_cap, max_seg_cap, false, false);
+        if (st)
+            return st;
+    }
+    cudaStream_t s = ctx->stream;
+    k_src_prefix<<<1, 256, 0, s>>>(d_src, P, in_off);
+    GCA_CHECK_LAUNCH(ctx);
+    k_src_bounds_init<<<grid_for(6 * P), kBlock, 0, s>>>(ord, P);
+    GCA_CHECK_LAUNCH(ctx);
+    const int gx = std::min(grid_for(max_seg_cap, kBlock * 4), ctx->num_sms * 4);
+    k_src_bounds<<<dim3(gx, P), kBlock, 0, s>>>(d_src, ord);
+    GCA_CHECK_LAUNCH(ctx);
+    k_voxel_layout<<<1, 256, 0, s>>>(ord, P, voxel, origin, lay, ctx->d_err);
+    GCA_CHECK_LAUNCH(ctx);
+    k_voxel_keys<<<dim3(gx, P), kBlock, 0, s>>>(d_src, in_off, origin, lay, voxel, sb.keys[0], sb.vals[0]);
+    GCA_CHECK_LAUNCH(ctx);
+    const int32_t *d_n = in_off + P;
+    int st = radix_sort(ctx, sb, d_n, total_cap, 64, nullptr);
+    if (st)
+        return st;
+    const int gs = std::min(grid_for(total_cap), ctx->num_sms * 8);
+    k_run_flags<<<gs, kBlock, 0, s>>>(sb, d_n, flags);
+    GCA_CHECK_LAUNCH(ctx);
+    st = exclusive_scan(ctx, flags, vid, d_n, total_cap, d_m);
+    if (st)
+        return st;
+    k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts);
+    GCA_CHECK_LAUNCH(ctx);
+    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0, sizeof(int32_t) * P, s));
+    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col,
+                                         seg_count);
+    GCA_CHECK_LAUNCH(ctx);
+    k_counts_to_offsets<<<1, 32, 0, s>>>(seg_count, P, out.seg_off);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+// copy segments into a contiguous batch (no downsampling)
+__global__ void k_gather(const SegSrc *src, const int32_t *off, float4 *pos, float4 *col, float4 *nrm)
+{
+    const int seg = blockIdx.y;
+    const int n = *src[seg].d_n;
+    const int base = off[seg];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        pos[base + i] = src[seg].pos[i];
+        col[base + i] = src[seg].col[i];
+        if (nrm)
+            nrm[base + i] = src[seg].nrm ? src[seg].nrm[i] : make_float4(0, 0, 0, 0);
+    }
+}
+
+int gather_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t max_seg_cap, Batch &out,
+                 bool with_normals)
+{
+    if (with_normals && !out.nrm)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gather_stage: batch has no normal storage");
+    k_src_prefix<<<1, 256, 0, ctx->stream>>>(d_src, P, out.seg_off);
+    GCA_CHECK_LAUNCH(ctx);
+    const int gx = std::min(grid_for(max_seg_cap, kBlock * 4), ctx->num_sms * 4);
+    k_gather<<<dim3(gx, P), kBlock, 0, ctx->stream>>>(d_src, out.seg_off, out.pos, out.col,
+                                                     with_normals ? out.nrm : nullptr);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+} // namespace gca3d

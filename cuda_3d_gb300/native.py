@@ -1,0 +1,345 @@
+"""ctypes binding of the gca3d C ABI (include/gca3d.h).
+
+This module is how Python (tests, bench) reaches the CUDA path: every call goes
+through the same extern "C" entry points a C or C++ caller uses.  There is no
+fallback: if libgca3d.so is missing or no CUDA device is present, loading fails
+loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgca3d.so")
+
+OK = 0
+ERR_INVALID_VALUE = 1
+ERR_OUT_OF_MEMORY = 2
+ERR_NO_CORRESPONDENCES = 3
+ERR_SINGULAR = 4
+ERR_TIMEOUT = 5
+ERR_CUDA = 6
+ERR_CAPACITY = 7
+ERR_NOT_SUPPORTED = 8
+
+FILTER_NONE, FILTER_ADAPTIVE, FILTER_FIXED = 0, 1, 2
+UPDATE_EULER_ZYX, UPDATE_SE3_EXP = 0, 1
+MAX_SCALES = 8
+
+
+class Intrinsics(C.Structure):
+    _fields_ = [("fx", C.c_float), ("fy", C.c_float), ("cx", C.c_float), ("cy", C.c_float)]
+
+
+class Extrinsics(C.Structure):
+    _fields_ = [("rotation", C.c_float * 9), ("translation", C.c_float * 3)]
+
+
+class Filter(C.Structure):
+    _fields_ = [("mode", C.c_int), ("radius", C.c_int), ("sigma_space", C.c_float), ("sigma_depth", C.c_float)]
+
+
+class ScaleParams(C.Structure):
+    _fields_ = [("voxel", C.c_float), ("max_iter", C.c_int), ("max_corr", C.c_float),
+                ("normal_radius", C.c_float), ("grad_radius", C.c_float), ("max_nn", C.c_int)]
+
+
+class IcpParams(C.Structure):
+    _fields_ = [("n_scales", C.c_int), ("scales", ScaleParams * MAX_SCALES), ("lambda_", C.c_float),
+                ("update_map", C.c_int), ("rot_eps", C.c_double), ("trans_eps", C.c_double),
+                ("compensated", C.c_int), ("use_graph", C.c_int), ("keep_target_normals", C.c_int)]
+
+
+class IcpResult(C.Structure):
+    _fields_ = [("T", C.c_double * 16), ("rmse_ref", C.c_double), ("fitness", C.c_double),
+                ("inlier_rmse", C.c_double), ("iterations", C.c_int), ("converged", C.c_int),
+                ("status", C.c_int), ("n_src", C.c_int), ("n_tgt", C.c_int)]
+
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_F = C.c_float
+_SIGS = {
+    "gca3d_create": [C.c_int, _P, C.POINTER(_P)],
+    "gca3d_destroy": [_P],
+    "gca3d_synchronize": [_P],
+    "gca3d_status_string": [C.c_int],
+    "gca3d_last_error": [_P],
+    "gca3d_kernel_launches": [_P],
+    "gca3d_stream": [_P],
+    "gca3d_device_alloc": [_P, _I64, C.POINTER(_P)],
+    "gca3d_device_free": [_P, _P],
+    "gca3d_copy": [_P, _P, _P, _I64],
+    "gca3d_cloud_create": [_P, _I64, C.POINTER(_P)],
+    "gca3d_cloud_destroy": [_P],
+    "gca3d_cloud_upload": [_P, _P, _P, _P, _I64],
+    "gca3d_cloud_set_normals": [_P, _P, _P, _I64],
+    "gca3d_cloud_set_gradients": [_P, _P, _P, _I64],
+    "gca3d_cloud_capacity": [_P, C.POINTER(_I64)],
+    "gca3d_cloud_size": [_P, _P, C.POINTER(_I64)],
+    "gca3d_cloud_has_normals": [_P, C.POINTER(C.c_int)],
+    "gca3d_cloud_download": [_P, _P, _P, _P, _P, _P, _I64, C.POINTER(_I64)],
+    "gca3d_cloud_device_views": [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)],
+    "gca3d_cloud_copy": [_P, _P, _P],
+    "gca3d_cloud_append": [_P, _P, _P],
+    "gca3d_bounds": [_P, _P, _P, _P],
+    "gca3d_transform": [_P, _P, _P],
+    "gca3d_frame_to_cloud": [_P, _P, _P, C.c_int, C.c_int, C.POINTER(Intrinsics), C.POINTER(Intrinsics),
+                             C.POINTER(Extrinsics), _F, _F, _F, C.POINTER(Filter), _P],
+    "gca3d_voxel_downsample": [_P, _P, _F, _P],
+    "gca3d_estimate_normals": [_P, _P, _F, C.c_int],
+    "gca3d_color_gradient": [_P, _P, _F],
+    "gca3d_nn_search": [_P, _P, _P, _F, _P],
+    "gca3d_radius_search": [_P, _P, _P, _F, _P, _P, _P, _P, _I64, C.POINTER(_I64)],
+    "gca3d_build_gauss_newton": [_P, _P, _P, _P, _F, _P, _P, C.POINTER(C.c_double)],
+    "gca3d_abs_residual": [_P, _P, _P, _P, _F, _P],
+    "gca3d_color_icp": [_P, _P, _P, C.POINTER(IcpParams), _P, C.POINTER(IcpResult)],
+    "gca3d_color_icp_batched": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), _P, _P],
+    "gca3d_icp_plan_create": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), C.POINTER(_P)],
+    "gca3d_icp_plan_execute": [_P, _P, _P],
+    "gca3d_icp_plan_destroy": [_P],
+    "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
+}
+_RESTYPES = {"gca3d_status_string": C.c_char_p, "gca3d_last_error": C.c_char_p,
+             "gca3d_kernel_launches": C.c_int64, "gca3d_stream": C.c_void_p}
+
+_lib = None
+
+
+def exported_symbols():
+    """the entry points include/gca3d.h declares"""
+    return sorted(_SIGS)
+
+
+def load(path=LIB_PATH):
+    """load libgca3d.so (raises if it was not built)"""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(path)
+    for name, args in _SIGS.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = _RESTYPES.get(name, C.c_int)
+    _lib = L
+    return L
+
+
+class GcaError(RuntimeError):
+    def __init__(self, status, detail):
+        super().__init__(f"gca3d status {status}: {detail}")
+        self.status = status
+
+
+def _ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """owns a gca3d_context; stream=None creates a private non-blocking stream"""
+
+    def __init__(self, device=0, stream=None):
+        self.L = load()
+        h = C.c_void_p()
+        st = self.L.gca3d_create(device, stream, C.byref(h))
+        if st != OK:
+            raise GcaError(st, self.L.gca3d_status_string(st).decode())
+        self.h = h
+
+    def check(self, st):
+        if st != OK:
+            raise GcaError(st, self.L.gca3d_last_error(self.h).decode())
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gca3d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        return self.check(self.L.gca3d_synchronize(self.h))
+
+    @property
+    def stream(self):
+        return self.L.gca3d_stream(self.h)
+
+    def launches(self):
+        return self.L.gca3d_kernel_launches(self.h)
+
+    # -- buffers ---------------------------------------------------------
+    def alloc(self, nbytes):
+        p = C.c_void_p()
+        self.check(self.L.gca3d_device_alloc(self.h, int(nbytes), C.byref(p)))
+        return DeviceBuffer(self, p, int(nbytes))
+
+    def cloud(self, capacity):
+        return Cloud(self, capacity)
+
+    def cloud_from(self, xyz, rgb=None, capacity=None):
+        xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+        c = Cloud(self, max(len(xyz), capacity or 0, 1))
+        c.upload(xyz, rgb)
+        return c
+
+
+class DeviceBuffer:
+    def __init__(self, ctx, ptr, nbytes):
+        self.ctx, self.ptr, self.nbytes = ctx, ptr, nbytes
+
+    def __del__(self):
+        try:
+            if self.ptr and self.ctx.h:
+                self.ctx.L.gca3d_device_free(self.ctx.h, self.ptr)
+        except Exception:
+            pass
+
+    def read(self, dtype, count):
+        out = np.empty(count, dtype)
+        if count:
+            self.ctx.check(self.ctx.L.gca3d_copy(self.ctx.h, _ptr(out), self.ptr, out.nbytes))
+        return out
+
+    def write(self, arr):
+        arr = np.ascontiguousarray(arr)
+        assert arr.nbytes <= self.nbytes
+        self.ctx.check(self.ctx.L.gca3d_copy(self.ctx.h, self.ptr, _ptr(arr), arr.nbytes))
+
+
+class Cloud:
+    def __init__(self, ctx, capacity):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        ctx.check(ctx.L.gca3d_cloud_create(ctx.h, int(capacity), C.byref(self.h)))
+        self.capacity = int(capacity)
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.L.gca3d_cloud_destroy(self.h)
+        except Exception:
+            pass
+
+    def upload(self, xyz, rgb=None):
+        xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+        rgb = None if rgb is None else np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+        self.ctx.check(self.ctx.L.gca3d_cloud_upload(self.ctx.h, self.h, _ptr(xyz), _ptr(rgb), len(xyz)))
+        return self
+
+    def set_normals(self, nrm):
+        nrm = np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+        self.ctx.check(self.ctx.L.gca3d_cloud_set_normals(self.ctx.h, self.h, _ptr(nrm), len(nrm)))
+
+    def set_gradients(self, grd):
+        grd = np.ascontiguousarray(grd, np.float32).reshape(-1, 3)
+        self.ctx.check(self.ctx.L.gca3d_cloud_set_gradients(self.ctx.h, self.h, _ptr(grd), len(grd)))
+
+    def __len__(self):
+        n = C.c_int64()
+        self.ctx.check(self.ctx.L.gca3d_cloud_size(self.ctx.h, self.h, C.byref(n)))
+        return n.value
+
+    def download(self, xyz=True, rgb=True, normals=False, grad=False):
+        n = len(self)
+        out = {k: np.empty((n, 3), np.float32) for k, w in (("xyz", xyz), ("rgb", rgb), ("normals", normals),
+                                                            ("grad", grad)) if w}
+        cnt = C.c_int64()
+        self.ctx.check(self.ctx.L.gca3d_cloud_download(
+            self.ctx.h, self.h, _ptr(out.get("xyz")), _ptr(out.get("rgb")), _ptr(out.get("normals")),
+            _ptr(out.get("grad")), n, C.byref(cnt)))
+        return out
+
+    def device_views(self):
+        v = [C.c_void_p() for _ in range(5)]
+        self.ctx.check(self.ctx.L.gca3d_cloud_device_views(self.h, *[C.byref(x) for x in v]))
+        return [x.value for x in v]
+
+
+def scale(voxel, max_iter, max_corr, normal_radius, grad_radius, max_nn=0):
+    return ScaleParams(voxel, max_iter, max_corr, normal_radius, grad_radius, max_nn)
+
+
+def icp_params(scales, lam=0.968, update_map=UPDATE_EULER_ZYX, rot_eps=1e-6, trans_eps=1e-6, compensated=True,
+               use_graph=False, keep_target_normals=False):
+    p = IcpParams()
+    p.n_scales = len(scales)
+    for i, s in enumerate(scales):
+        p.scales[i] = s if isinstance(s, ScaleParams) else ScaleParams(*s)
+    p.lambda_ = lam
+    p.update_map = update_map
+    p.rot_eps = rot_eps
+    p.trans_eps = trans_eps
+    p.compensated = int(compensated)
+    p.use_graph = int(use_graph)
+    p.keep_target_normals = int(keep_target_normals)
+    return p
+
+
+def result_dict(r):
+    return dict(T=np.array(r.T[:]).reshape(4, 4), rmse_ref=r.rmse_ref, fitness=r.fitness,
+                inlier_rmse=r.inlier_rmse, iterations=r.iterations, converged=bool(r.converged),
+                status=r.status, n_src=r.n_src, n_tgt=r.n_tgt)
+
+
+def cloud_array(clouds):
+    arr = (C.c_void_p * len(clouds))(*[c.h.value for c in clouds])
+    return arr
+
+
+class IcpPlan:
+    """a reusable (optionally graph-captured) schedule over fixed clouds"""
+
+    def __init__(self, ctx, src, tgt, params):
+        self.ctx = ctx
+        self.src, self.tgt = list(src), list(tgt)
+        self.h = C.c_void_p()
+        self._sa, self._ta = cloud_array(self.src), cloud_array(self.tgt)
+        ctx.check(ctx.L.gca3d_icp_plan_create(ctx.h, len(self.src), self._sa, self._ta, C.byref(params),
+                                              C.byref(self.h)))
+        self.P = len(self.src)
+        self._res = (IcpResult * self.P)()
+
+    def execute(self, T_init=None, results=True):
+        Ti = None
+        if T_init is not None:
+            Ti = np.ascontiguousarray(np.asarray(T_init, np.float64).reshape(self.P, 16))
+        self.ctx.check(self.ctx.L.gca3d_icp_plan_execute(self.h, _ptr(Ti), self._res if results else None))
+        return [result_dict(r) for r in self._res] if results else None
+
+    def kernels(self):
+        n = C.c_int64()
+        self.ctx.check(self.ctx.L.gca3d_icp_plan_kernels(self.h, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.L.gca3d_icp_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
+def color_icp(ctx, src, tgt, params, T_init=None):
+    r = IcpResult()
+    Ti = None if T_init is None else np.ascontiguousarray(np.asarray(T_init, np.float64).reshape(16))
+    ctx.check(ctx.L.gca3d_color_icp(ctx.h, src.h, tgt.h, C.byref(params), _ptr(Ti), C.byref(r)))
+    return result_dict(r)
+
+
+def color_icp_batched(ctx, srcs, tgts, params, T_init=None):
+    P = len(srcs)
+    res = (IcpResult * P)()
+    Ti = None if T_init is None else np.ascontiguousarray(np.asarray(T_init, np.float64).reshape(P, 16))
+    ctx.check(ctx.L.gca3d_color_icp_batched(ctx.h, P, cloud_array(srcs), cloud_array(tgts), C.byref(params),
+                                            _ptr(Ti), res))
+    return [result_dict(r) for r in res]

@@ -299,13 +299,14 @@ def _raycast(scene, o, d):
         best = np.where(ok, tmin, best)
         sid = np.where(ok, k, sid)
         k += 1
+    dd = (d * d).sum(1)
     for c, r in scene["spheres"]:
         oc = o - c
         b = (oc * d).sum(1)
         cc = (oc * oc).sum(1) - r * r
-        disc = b * b - cc
+        disc = b * b - dd * cc
         with np.errstate(invalid="ignore"):
-            t = -b - np.sqrt(disc)
+            t = (-b - np.sqrt(disc)) / dd
         ok = (disc >= 0) & (t > 1e-6) & (t < best)
         best = np.where(ok, t, best)
         sid = np.where(ok, k, sid)
@@ -317,7 +318,9 @@ def render_rgbd(scene, T_cam, seed, cam=Camera(), zero_frac=0.05, color_noise=4.
     """depth (uint16 mm, H x W) and BGR8 (H x W x 3) seen from camera pose T_cam
     (camera -> scene frame).  Depth noise N(0, (0.002 z^2)^2) m."""
     rng = np.random.default_rng(seed)
-    u, v = np.meshgrid(np.arange(cam.width, dtype=np.float64), np.arange(cam.height, dtype=np.float64))
+    # pixel (x, y) looks along (x - 0.5, y - 0.5): the reference back-projects with
+    # that half-pixel shift (cuda_point_cloud_factory.cu:232)
+    u, v = np.meshgrid(np.arange(cam.width, dtype=np.float64) - 0.5, np.arange(cam.height, dtype=np.float64) - 0.5)
     dcam = np.stack([(u - cam.cx) / cam.fx, (v - cam.cy) / cam.fy, np.ones_like(u)], -1).reshape(-1, 3)
     R, t = T_cam[:3, :3], T_cam[:3, 3]
     dw = dcam @ R.T

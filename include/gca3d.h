@@ -1,0 +1,252 @@
+/*
+ * gca3d.h -- C ABI of the GB300-native RGB-D registration path.
+ *
+ * Replaces the GPU entry points of XssZuiNB/CUDA_3D's registration path (the
+ * reference exposes them as C++ classes and free functions returning
+ * cudaError_t; each declaration below names the reference interface it stands
+ * in for).  Every call is stream-ordered on the context's stream and returns an
+ * int status (GCA3D_OK = 0).  Clouds are opaque device-resident handles owned by
+ * the caller; pointers marked "device" are device pointers, every other pointer
+ * is host memory unless stated.  A context belongs to one host thread at a time.
+ *
+ * Layout of a cloud on the device (structure of arrays, 16-byte elements):
+ *   pos  float4 {x, y, z, intensity}   intensity = 0.2126 r + 0.7152 g + 0.0722 b
+ *   col  float4 {r, g, b, 0}           colours in [0, 1]
+ *   nrm  float4 {nx, ny, nz, 0}        after gca3d_estimate_normals
+ *   grd  float4 {gx, gy, gz, 0}        after gca3d_color_gradient
+ * The point count lives on the device so that variable-size stages need no host
+ * round trip; gca3d_cloud_size reads it back.
+ */
+#ifndef GCA3D_H
+#define GCA3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (reference: cudaError_t returns and false/nullptr results,
+ *      e.g. src/registration/cuda_color_icp_build_least_square.cu:438-452) ---- */
+#define GCA3D_OK 0
+#define GCA3D_ERR_INVALID_VALUE 1
+#define GCA3D_ERR_OUT_OF_MEMORY 2
+#define GCA3D_ERR_NO_CORRESPONDENCES 3
+#define GCA3D_ERR_SINGULAR 4
+#define GCA3D_ERR_TIMEOUT 5
+#define GCA3D_ERR_CUDA 6
+#define GCA3D_ERR_CAPACITY 7
+#define GCA3D_ERR_NOT_SUPPORTED 8
+
+typedef struct gca3d_context gca3d_context;
+typedef struct gca3d_cloud gca3d_cloud;
+typedef struct gca3d_icp_plan gca3d_icp_plan;
+
+/* camera model (reference: src/camera/camera_param.hpp:5-18) */
+typedef struct {
+    float fx, fy, cx, cy;
+} gca3d_intrinsics;
+
+/* rotation column-major, as the reference stores it */
+typedef struct {
+    float rotation[9];
+    float translation[3];
+} gca3d_extrinsics;
+
+#define GCA3D_FILTER_NONE 0
+#define GCA3D_FILTER_ADAPTIVE 1 /* the reference's adaptive bilateral filter */
+#define GCA3D_FILTER_FIXED 2    /* fixed window: radius, sigma_space (px), sigma_depth (depth units) */
+
+typedef struct {
+    int mode;
+    int radius;
+    float sigma_space;
+    float sigma_depth;
+} gca3d_filter;
+
+#define GCA3D_UPDATE_EULER_ZYX 0 /* R = Rz Ry Rx, t = x[3..5] (reference eigen_solver.hpp:30-40) */
+#define GCA3D_UPDATE_SE3_EXP 1   /* SE(3) exponential */
+
+#define GCA3D_MAX_SCALES 8
+
+/* one level of the coarse-to-fine schedule.  voxel <= 0 uses the clouds as
+ * given (the reference's single-level color_icp::align). */
+typedef struct {
+    float voxel;
+    int max_iter;
+    float max_corr;
+    float normal_radius;
+    float grad_radius;
+    int max_nn; /* 0 = every neighbour inside normal_radius (reference) */
+} gca3d_scale;
+
+typedef struct {
+    int n_scales;
+    gca3d_scale scales[GCA3D_MAX_SCALES];
+    float lambda;      /* geometric weight, 0.968 in the reference (color_icp.hpp:46) */
+    int update_map;    /* GCA3D_UPDATE_* */
+    double rot_eps;    /* converged when cos(step angle) >= 1 - rot_eps ... */
+    double trans_eps;  /* ... and |step translation|^2 <= trans_eps (color_icp.hpp:47-48) */
+    int compensated;   /* 1: Kahan FP32 in each block, FP64 across blocks; 0: plain FP32 */
+    int use_graph;     /* 1: replay the whole schedule as one CUDA graph */
+    int keep_target_normals; /* 1 with voxel <= 0: use the normals already on the target */
+} gca3d_icp_params;
+
+typedef struct {
+    double T[16];       /* row-major 4x4, maps source onto target */
+    double rmse_ref;    /* sum of squared weighted residuals / N_src of the last built
+                           system (reference color_icp::get_RSME, color_icp.cu:231) */
+    double fitness;     /* correspondences / N_src, last built system */
+    double inlier_rmse; /* sqrt(mean squared point distance over correspondences) */
+    int iterations;     /* summed over scales */
+    int converged;      /* the last scale met the convergence test */
+    int status;         /* GCA3D_OK, NO_CORRESPONDENCES, SINGULAR, TIMEOUT */
+    int n_src;          /* source points at the last scale */
+    int n_tgt;          /* target points at the last scale */
+} gca3d_icp_result;
+
+/* ---------------------------------------------------------------------------
+ * context and clouds
+ * ------------------------------------------------------------------------- */
+
+/* stream: a cudaStream_t, or NULL for a new non-blocking stream owned by the context */
+int gca3d_create(int device, void *stream, gca3d_context **ctx);
+int gca3d_destroy(gca3d_context *ctx);
+int gca3d_synchronize(gca3d_context *ctx);
+const char *gca3d_status_string(int status);
+/* detail of the last failure on this context (static storage, overwritten) */
+const char *gca3d_last_error(gca3d_context *ctx);
+/* number of kernels this library launched on the context since creation */
+int64_t gca3d_kernel_launches(gca3d_context *ctx);
+/* the context's stream (cudaStream_t) */
+void *gca3d_stream(gca3d_context *ctx);
+/* plain device buffers for callers without their own allocator */
+int gca3d_device_alloc(gca3d_context *ctx, int64_t bytes, void **ptr);
+int gca3d_device_free(gca3d_context *ctx, void *ptr);
+/* stream-ordered copy between any two pointers (host or device); synchronises */
+int gca3d_copy(gca3d_context *ctx, void *dst, const void *src, int64_t bytes);
+
+/* reference: gca::point_cloud(size_t) (src/geometry/point_cloud.hpp:26) */
+int gca3d_cloud_create(gca3d_context *ctx, int64_t capacity, gca3d_cloud **cloud);
+int gca3d_cloud_destroy(gca3d_cloud *cloud);
+/* xyz, rgb: n x 3 floats, host or device memory.  rgb may be NULL (black).
+ * reference: point_cloud::create_from_pcl (src/geometry/point_cloud.cu:481-504) */
+int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *cloud, const float *xyz,
+                       const float *rgb, int64_t n);
+/* normals (n x 3) supplied by the caller; marks the cloud as having normals */
+int gca3d_cloud_set_normals(gca3d_context *ctx, gca3d_cloud *cloud, const float *nrm, int64_t n);
+/* colour gradients (n x 3) supplied by the caller; needs normals */
+int gca3d_cloud_set_gradients(gca3d_context *ctx, gca3d_cloud *cloud, const float *grd, int64_t n);
+int gca3d_cloud_capacity(const gca3d_cloud *cloud, int64_t *capacity);
+/* reads the device-side count (synchronises) */
+int gca3d_cloud_size(gca3d_context *ctx, gca3d_cloud *cloud, int64_t *n);
+int gca3d_cloud_has_normals(const gca3d_cloud *cloud, int *has);
+/* any output pointer may be NULL; each is n x 3 floats of host or device memory.
+ * reference: point_cloud::download / download_normals (point_cloud.cu:75-91) */
+int gca3d_cloud_download(gca3d_context *ctx, gca3d_cloud *cloud, float *xyz, float *rgb,
+                         float *nrm, float *grd, int64_t cap, int64_t *n);
+/* raw device views (float4 SoA) and the device count */
+int gca3d_cloud_device_views(gca3d_cloud *cloud, void **pos, void **col, void **nrm,
+                             void **grd, int32_t **d_count);
+/* reference: point_cloud::operator= (point_cloud.cu:39-50) */
+int gca3d_cloud_copy(gca3d_context *ctx, const gca3d_cloud *src, gca3d_cloud *dst);
+/* reference: point_cloud::operator+= (point_cloud.cu:55-73) */
+int gca3d_cloud_append(gca3d_context *ctx, gca3d_cloud *dst, const gca3d_cloud *src);
+
+/* ---------------------------------------------------------------------------
+ * path stages
+ * ------------------------------------------------------------------------- */
+
+/* AABB of the cloud (true max; the reference starts its max at FLT_MIN).
+ * reference: cuda_compute_min_max_bound (src/geometry/geometry_util.cuh:88-105) */
+int gca3d_bounds(gca3d_context *ctx, gca3d_cloud *cloud, float mn[3], float mx[3]);
+
+/* p <- R p + t, n <- R n; T row-major 4x4.
+ * reference: point_cloud::transform (src/geometry/point_cloud.cu:93-105) */
+int gca3d_transform(gca3d_context *ctx, gca3d_cloud *cloud, const double T[16]);
+
+/* depth (uint16, h x w) and BGR8 colour (h x w x 3) in device memory -> cloud of the
+ * valid pixels in raster order.  reference: point_cloud::create_from_rgbd
+ * (src/geometry/point_cloud.cu:455-479) / cuda_make_point_cloud
+ * (src/geometry/cuda_point_cloud_factory.cu:269-313) */
+int gca3d_frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr, int w,
+                         int h, const gca3d_intrinsics *depth_intrin,
+                         const gca3d_intrinsics *color_intrin,
+                         const gca3d_extrinsics *depth_to_color, float depth_scale, float tmin,
+                         float tmax, const gca3d_filter *filter, gca3d_cloud *out);
+
+/* reference: point_cloud::voxel_grid_down_sample (src/geometry/point_cloud.cu:198-229),
+ * cuda_voxel_grid_downsample (src/geometry/cuda_voxel_grid_down_sample.cu:123-161) */
+int gca3d_voxel_downsample(gca3d_context *ctx, gca3d_cloud *in, float voxel, gca3d_cloud *out);
+
+/* reference: point_cloud::estimate_normals (src/geometry/point_cloud.cu:145-181),
+ * cuda_estimate_normals (src/geometry/cuda_estimate_normals.cu:153-199).
+ * max_nn > 0 keeps the max_nn nearest neighbours (distance, then index). */
+int gca3d_estimate_normals(gca3d_context *ctx, gca3d_cloud *cloud, float radius, int max_nn);
+
+/* reference: cuda_compute_color_gradient
+ * (src/registration/cuda_compute_color_gradient.cu:92-127); needs normals */
+int gca3d_color_gradient(gca3d_context *ctx, gca3d_cloud *cloud, float radius);
+
+/* nearest reference point within radius for every query point, -1 if none; ties on
+ * distance go to the smaller index.  out_idx: device int32[n_query].
+ * reference: point_cloud::nn_search (src/geometry/point_cloud.cu:506-557),
+ * cuda_nn_search (src/geometry/cuda_nn_search.cu:545-619) */
+int gca3d_nn_search(gca3d_context *ctx, gca3d_cloud *query, gca3d_cloud *ref, float radius,
+                    int32_t *out_idx);
+
+/* neighbour lists inside radius (self included), in the reference's scan order for
+ * the given grid origin (NULL: the reference's normal-estimation bounds).
+ * counts/starts: device int32[n_query]; list: device int32[list_cap]; *total is
+ * written on the host (synchronises).  reference: cuda_search_radius_neighbors
+ * (src/geometry/cuda_nn_search.cu:622-723) */
+int gca3d_radius_search(gca3d_context *ctx, gca3d_cloud *query, gca3d_cloud *ref, float radius,
+                        const float grid_min[3], int32_t *counts, int32_t *starts,
+                        int32_t *list, int64_t list_cap, int64_t *total);
+
+/* Gauss-Newton system of the colored-ICP objective for given correspondences
+ * (device int32[n_src]); jtj row-major 6x6, all outputs host memory.
+ * reference: cuda_build_gauss_newton_color_icp
+ * (src/registration/cuda_color_icp_build_least_square.cu:431-474) */
+int gca3d_build_gauss_newton(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt,
+                             const int32_t *nn, float lambda, double jtj[36], double jtr[6],
+                             double *r2);
+
+/* |r_geometric| + |r_colour| per source point (device float[n_src]).
+ * reference: cuda_compute_abs_residual_color_icp
+ * (src/registration/cuda_color_icp_build_least_square.cu:310-350) */
+int gca3d_abs_residual(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt, const int32_t *nn,
+                       float lambda, float *out);
+
+/* the colored ICP of one pair, optionally coarse to fine; T_init may be NULL.
+ * The source cloud is not modified.  reference: color_icp::align
+ * (src/registration/color_icp.cu:151-234) */
+int gca3d_color_icp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt,
+                    const gca3d_icp_params *params, const double T_init[16],
+                    gca3d_icp_result *result);
+
+/* many pairs of uneven size in one batched schedule (every stage launched once
+ * for all pairs).  T_init: n_pairs x 16 or NULL.  No reference counterpart (the
+ * reference aligns one pair per call). */
+int gca3d_color_icp_batched(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src,
+                            gca3d_cloud *const *tgt, const gca3d_icp_params *params,
+                            const double *T_init, gca3d_icp_result *results);
+
+/* a reusable plan: workspace allocated and (with use_graph) the whole schedule
+ * captured once; execute replays it on the clouds' current contents.  No
+ * reference counterpart. */
+int gca3d_icp_plan_create(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src,
+                          gca3d_cloud *const *tgt, const gca3d_icp_params *params,
+                          gca3d_icp_plan **plan);
+/* T_init: n_pairs x 16 host doubles or NULL (identity); results may be NULL, in
+ * which case execute does not synchronise */
+int gca3d_icp_plan_execute(gca3d_icp_plan *plan, const double *T_init,
+                           gca3d_icp_result *results);
+int gca3d_icp_plan_destroy(gca3d_icp_plan *plan);
+/* kernels one execute launches (graph nodes, or the eager launches of the last run) */
+int gca3d_icp_plan_kernels(gca3d_icp_plan *plan, int64_t *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -93,9 +93,42 @@ void orc_aabb(const float *xyz, int64_t n, int flt_min_bug, float mn[3], float m
 /* a1-a3: depth filter + back-projection                               */
 /* ------------------------------------------------------------------ */
 
+/* exp(x) in FP32 by Cody-Waite range reduction (x = k ln2 + r, |r| <= ln2/2, ln2
+ * split in a 16-bit head and a tail so k * head is exact) and a degree-7 Taylor
+ * polynomial in Horner form, scaled by 2^k in two exact steps.  Plain IEEE
+ * multiply/add only, so the CUDA kernel evaluates the identical sequence and the
+ * filtered depths agree bit for bit; at most 2 ulp from exp(x). */
+static float orc_expf(float x)
+{
+    if (x != x)
+        return x;
+    if (x > 88.72283935546875f)
+        return INFINITY;
+    if (x < -103.972084045410156f)
+        return 0.0f;
+    const float kf = rintf(x * 1.44269502162933349609f);
+    const float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187045e-06f;
+    float p = 1.0f / 5040.0f;
+    p = p * r + 1.0f / 720.0f;
+    p = p * r + 1.0f / 120.0f;
+    p = p * r + 1.0f / 24.0f;
+    p = p * r + 1.0f / 6.0f;
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    int k = (int)kf;
+    int k1 = k / 2, k2 = k - k / 2;
+    union { uint32_t u; float f; } a, b;
+    a.u = (uint32_t)(k1 + 127) << 23;
+    b.u = (uint32_t)(k2 + 127) << 23;
+    return (p * a.f) * b.f;
+}
+
+float orc_exp32(float x) { return orc_expf(x); }
+
 /* __gaussian / __gaussian_square (cuda_point_cloud_factory.cu:19-27) */
-static inline float gauss(float x, float sigma) { return expf(-(x * x) / (sigma * sigma)); }
-static inline float gauss_sq(float x2, float sigma) { return expf(-x2 / (sigma * sigma)); }
+static inline float gauss(float x, float sigma) { return orc_expf(-(x * x) / (sigma * sigma)); }
+static inline float gauss_sq(float x2, float sigma) { return orc_expf(-x2 / (sigma * sigma)); }
 
 /* zero-skipping bilateral filter (cuda_point_cloud_factory.cu:64-98) */
 static float bilateral(const uint16_t *in, int w, int h, int x, int y, uint16_t centre,
@@ -141,6 +174,19 @@ static float filter_pixel(const uint16_t *in, int w, int h, float depth_scale, i
     return bilateral(in, w, h, x, y, d, (int)r, ss, sd);
 }
 
+/* float -> int truncation with the GPU's conversion semantics (NaN -> 0,
+ * saturation), which (int) in C leaves undefined */
+static inline int f2i_rz(float x)
+{
+    if (x != x)
+        return 0;
+    if (x >= 2147483647.0f)
+        return 2147483647;
+    if (x <= -2147483648.0f)
+        return (-2147483647 - 1);
+    return (int)x;
+}
+
 /* __kernel_make_pointcloud_Z16_BGR8 (cuda_point_cloud_factory.cu:189-267) and
  * remove_invalid_points (geometry_util.cuh:124-130, stable) */
 int64_t orc_make_point_cloud(const uint16_t *depth, const uint8_t *bgr, int w, int h,
@@ -177,7 +223,7 @@ int64_t orc_make_point_cloud(const uint16_t *depth, const uint8_t *bgr, int w, i
         float cz = R[2] * X + R[5] * Y + R[8] * z + t[2];
         float cu = (cx * ci->fx / cz) + ci->cx;
         float cv = (cy * ci->fy / cz) + ci->cy;
-        int tx = (int)(cu + 0.5f), ty = (int)(cv + 0.5f);
+        int tx = f2i_rz(cu + 0.5f), ty = f2i_rz(cv + 0.5f);
         if (tx < 0 || tx >= w || ty < 0 || ty >= h)
             continue;
         int64_t c = 3 * ((int64_t)ty * w + tx);

@@ -41,6 +41,9 @@ enum { ORC_UPDATE_EULER_ZYX = 0, ORC_UPDATE_SE3_EXP = 1 };
 void orc_set_threads(int n);
 int orc_get_threads(void);
 
+/* the FP32 exp used by the depth filter (same operation sequence on the GPU) */
+float orc_exp32(float x);
+
 /* color3::to_intensity (geometry/type.hpp:45-51): FP64 weighted sum rounded to float */
 float orc_intensity(float r, float g, float b);
 

@@ -70,6 +70,7 @@ def _bind(L):
         "orc_set_threads": (v, [C.c_int]),
         "orc_get_threads": (C.c_int, []),
         "orc_intensity": (C.c_float, [C.c_float, C.c_float, C.c_float]),
+        "orc_exp32": (C.c_float, [C.c_float]),
         "orc_aabb": (v, [F32, i64, C.c_int, F32, F32]),
         "orc_make_point_cloud": (i64, [U16, U8, C.c_int, C.c_int, C.POINTER(Intrinsics),
                                        C.POINTER(Intrinsics), C.POINTER(Extrinsics), C.c_float,
@@ -105,6 +106,11 @@ def _f32(a, cols=3):
 
 def set_threads(n):
     lib().orc_set_threads(int(n))
+
+
+def exp32(x):
+    f = lib().orc_exp32
+    return np.array([f(float(v)) for v in np.asarray(x, np.float32).reshape(-1)], np.float32)
 
 
 def intensity(rgb):

@@ -1,0 +1,337 @@
+"""GPU parity of the individual path stages, called through the C ABI.
+
+Bit-exact against the oracle / the reference's own outputs (golden fixtures) for
+keys, indices, neighbour lists, the voxel set and the rigid transform; within the
+stated tolerances of the FP64 oracle for normals, gradients and the
+Gauss-Newton system."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def N():
+    from cuda_3d_gb300 import build, native
+
+    build.build()
+    return native
+
+
+@pytest.fixture(scope="module")
+def ctx(N):
+    return N.Context(0)
+
+
+@pytest.fixture(scope="module")
+def room():
+    from cuda_3d_gb300 import synth
+
+    rng = np.random.default_rng(77)
+    return synth.sample_room(synth.room_scene(1234), 250_000, rng)
+
+
+def angle_err(a, b):
+    a = a / np.maximum(np.linalg.norm(a, axis=1, keepdims=True), 1e-30)
+    b = b / np.maximum(np.linalg.norm(b, axis=1, keepdims=True), 1e-30)
+    return np.arccos(np.clip(np.abs((a * b).sum(1)), -1, 1))
+
+
+# --------------------------------------------------------------------------- #
+# cloud basics
+# --------------------------------------------------------------------------- #
+def test_upload_download_roundtrip(ctx, golden, orc):
+    xyz, rgb = golden["cloud_xyz"], golden["cloud_rgb"]
+    c = ctx.cloud_from(xyz, rgb)
+    assert len(c) == len(xyz)
+    d = c.download()
+    np.testing.assert_array_equal(d["xyz"], xyz)
+    np.testing.assert_array_equal(d["rgb"], rgb)
+
+
+def test_bounds_true_max(ctx, golden):
+    for pts in (golden["cloud_xyz"], golden.voxel_input("neg05")[0]):
+        c = ctx.cloud_from(pts)
+        mn, mx = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        ctx.check(ctx.L.gca3d_bounds(ctx.h, c.h, mn.ctypes.data, mx.ctypes.data))
+        np.testing.assert_array_equal(mn, pts.min(0))
+        np.testing.assert_array_equal(mx, pts.max(0))  # the reference's FLT_MIN start is not reproduced
+
+
+def test_transform_bit_exact(ctx, golden):
+    c = ctx.cloud_from(golden.patch_xyz[:3000])
+    T = golden["transform_T"].astype(np.float64)
+    ctx.check(ctx.L.gca3d_transform(ctx.h, c.h, T.ctypes.data))
+    np.testing.assert_array_equal(c.download()["xyz"], golden["transform_out"])
+
+
+# --------------------------------------------------------------------------- #
+# voxel downsample: bit-exact
+# --------------------------------------------------------------------------- #
+def voxel_gpu(ctx, xyz, rgb, v):
+    c = ctx.cloud_from(xyz, rgb)
+    out = ctx.cloud(c.capacity)
+    ctx.check(ctx.L.gca3d_voxel_downsample(ctx.h, c.h, float(v), out.h))
+    return out.download()
+
+
+@pytest.mark.parametrize("tag", ["v05", "v02", "neg05", "dup", "one"])
+def test_voxel_golden(ctx, golden, tag):
+    xyz, rgb = golden.voxel_input(tag)
+    d = voxel_gpu(ctx, xyz, rgb, golden[f"voxel_{tag}_size"])
+    np.testing.assert_array_equal(d["xyz"], golden[f"voxel_{tag}_xyz"])
+    np.testing.assert_array_equal(d["rgb"], golden[f"voxel_{tag}_rgb"])
+
+
+@pytest.mark.parametrize("v", [0.04, 0.02, 0.01, 0.005])
+def test_voxel_full_size_vs_oracle(ctx, orc, room, v):
+    xyz, rgb = room
+    d = voxel_gpu(ctx, xyz, rgb, v)
+    ox, oc, cnt, _ = orc.voxel_downsample(xyz, rgb, v)
+    np.testing.assert_array_equal(d["xyz"], ox)
+    np.testing.assert_array_equal(d["rgb"], oc)
+
+
+def test_voxel_empty_and_invalid(ctx, N):
+    c = ctx.cloud(16)
+    out = ctx.cloud(16)
+    ctx.check(ctx.L.gca3d_voxel_downsample(ctx.h, c.h, 0.05, out.h))
+    assert len(out) == 0
+    assert ctx.L.gca3d_voxel_downsample(ctx.h, c.h, 0.0, out.h) == N.ERR_INVALID_VALUE
+    assert ctx.L.gca3d_voxel_downsample(ctx.h, c.h, -1.0, out.h) == N.ERR_INVALID_VALUE
+    small = ctx.cloud(4)
+    assert ctx.L.gca3d_voxel_downsample(ctx.h, c.h, 0.05, small.h) == N.ERR_CAPACITY
+
+
+def test_voxel_extent_beyond_key_range(ctx, N):
+    pts = np.array([[0, 0, 0], [1.0e5, 0, 0]], np.float32)
+    c = ctx.cloud_from(pts)
+    out = ctx.cloud(2)
+    assert ctx.L.gca3d_voxel_downsample(ctx.h, c.h, 0.001, out.h) == N.ERR_CAPACITY
+
+
+# --------------------------------------------------------------------------- #
+# nearest neighbour and radius lists: bit-exact
+# --------------------------------------------------------------------------- #
+def nn_gpu(ctx, q, r, radius):
+    cq, cr = ctx.cloud_from(q), ctx.cloud_from(r)
+    buf = ctx.alloc(4 * len(q))
+    ctx.check(ctx.L.gca3d_nn_search(ctx.h, cq.h, cr.h, float(radius), buf.ptr))
+    return buf.read(np.int32, len(q))
+
+
+def test_nn_golden(ctx, golden, orc):
+    idx = nn_gpu(ctx, golden["nn_q"], golden.nn_r, golden["nn_radius"])
+    np.testing.assert_array_equal(idx, golden["nn_idx"])
+
+
+def test_nn_exact_ties_min_index(ctx, golden, orc):
+    q, r, rad = golden["nntie_q"], golden["nntie_r"], float(golden["nntie_radius"])
+    idx = nn_gpu(ctx, q, r, rad)
+    np.testing.assert_array_equal(idx, orc.nn_search(q, r, rad, tie=orc.TIE_MIN_INDEX))
+
+
+def test_nn_full_size_vs_oracle(ctx, orc, room):
+    xyz = room[0]
+    rng = np.random.default_rng(5)
+    q = (xyz[:100_000] + rng.normal(scale=0.01, size=(100_000, 3))).astype(np.float32)
+    r = xyz[100_000:]
+    for rad in (0.015, 0.05):
+        idx = nn_gpu(ctx, q, r, rad)
+        np.testing.assert_array_equal(idx, orc.nn_search(q, r, rad, tie=orc.TIE_MIN_INDEX))
+
+
+def test_nn_queries_outside_grid(ctx, orc):
+    r = np.random.default_rng(1).random((1000, 3)).astype(np.float32)
+    q = np.array([[50, 50, 50], [-50, 0, 0], [0.5, 0.5, 0.5], [np.nan, 0, 0]], np.float32)
+    idx = nn_gpu(ctx, q, r, 0.1)
+    assert idx[0] == -1 and idx[1] == -1 and idx[3] == -1
+    assert idx[2] == orc.nn_search(q[2:3], r, 0.1)[0]
+
+
+def radius_gpu(ctx, q, r, radius, grid_min):
+    cq, cr = ctx.cloud_from(q), ctx.cloud_from(r)
+    n = len(q)
+    counts, starts = ctx.alloc(4 * n), ctx.alloc(4 * n)
+    cap = 256 * n
+    lst = ctx.alloc(4 * cap)
+    total = C.c_int64()
+    gm = None if grid_min is None else np.ascontiguousarray(grid_min, np.float32)
+    ctx.check(ctx.L.gca3d_radius_search(ctx.h, cq.h, cr.h, float(radius), None if gm is None else gm.ctypes.data,
+                                        counts.ptr, starts.ptr, lst.ptr, cap, C.byref(total)))
+    return counts.read(np.int32, n), starts.read(np.int32, n), lst.read(np.int32, total.value)
+
+
+@pytest.mark.parametrize("given", [True, False])
+def test_radius_lists_golden_order(ctx, golden, given):
+    pts = golden.patch_xyz
+    c, s, l = radius_gpu(ctx, pts, pts, golden["radius_r"], golden["radius_grid_min"] if given else None)
+    np.testing.assert_array_equal(c, golden["radius_counts"])
+    np.testing.assert_array_equal(s, golden["radius_starts"])
+    np.testing.assert_array_equal(l, golden["radius_list"])
+
+
+def test_radius_capacity_error(ctx, golden, N):
+    pts = golden.patch_xyz
+    cq = ctx.cloud_from(pts)
+    n = len(pts)
+    counts, starts, lst = ctx.alloc(4 * n), ctx.alloc(4 * n), ctx.alloc(64)
+    total = C.c_int64()
+    st = ctx.L.gca3d_radius_search(ctx.h, cq.h, cq.h, float(golden["radius_r"]), None, counts.ptr, starts.ptr,
+                                   lst.ptr, 16, C.byref(total))
+    assert st == N.ERR_CAPACITY and total.value == golden["radius_list"].size
+
+
+# --------------------------------------------------------------------------- #
+# normals and colour gradients: tolerance vs FP64
+# --------------------------------------------------------------------------- #
+@pytest.fixture(scope="module")
+def room_v01(orc, room):
+    vx, vc, _, _ = orc.voxel_downsample(room[0], room[1], 0.01)
+    return vx, vc
+
+
+def normals_gpu(ctx, xyz, radius, max_nn=0):
+    c = ctx.cloud_from(xyz)
+    ctx.check(ctx.L.gca3d_estimate_normals(ctx.h, c.h, float(radius), int(max_nn)))
+    return c.download(xyz=False, rgb=False, normals=True)["normals"]
+
+
+@pytest.mark.parametrize("max_nn", [0, 30])
+def test_normals_vs_f64(ctx, orc, room_v01, max_nn):
+    xyz = room_v01[0]
+    n = normals_gpu(ctx, xyz, 0.02, max_nn)
+    ref = orc.normals_f64(xyz, 0.02, max_nn)
+    zero_g, zero_r = np.linalg.norm(n, axis=1) == 0, np.linalg.norm(ref, axis=1) == 0
+    np.testing.assert_array_equal(zero_g, zero_r)
+    ok = ~zero_r
+    err = angle_err(n[ok].astype(np.float64), ref[ok])
+    # well-conditioned points match to 1e-3 rad; the sign follows n_z <= 0
+    assert np.percentile(err, 99) < 1e-3, np.percentile(err, [50, 99, 100])
+    assert np.median(err) < 1e-5
+    sign_ok = (n[ok, 2] <= 0) | (np.abs(n[ok, 2]) < 1e-6)
+    assert sign_ok.all()
+    np.testing.assert_allclose(np.linalg.norm(n[ok], axis=1), 1.0, atol=1e-5)
+
+
+def test_gradient_vs_f64(ctx, orc, room_v01):
+    xyz, rgb = room_v01
+    c = ctx.cloud_from(xyz, rgb)
+    ctx.check(ctx.L.gca3d_estimate_normals(ctx.h, c.h, 0.02, 0))
+    ctx.check(ctx.L.gca3d_color_gradient(ctx.h, c.h, 0.02))
+    d = c.download(xyz=False, rgb=False, normals=True, grad=True)
+    ref = orc.gradient_f64(xyz, rgb, d["normals"].astype(np.float64), 0.02)
+    g = d["grad"].astype(np.float64)
+    scale = np.maximum(np.linalg.norm(ref, axis=1), 1e-3)
+    rel = np.linalg.norm(g - ref, axis=1) / scale
+    assert np.percentile(rel, 99) < 1e-3, np.percentile(rel, [50, 99, 100])
+    np.testing.assert_array_equal(np.linalg.norm(g, axis=1) == 0, np.linalg.norm(ref, axis=1) == 0)
+
+
+def test_gradient_needs_normals(ctx, N, golden):
+    c = ctx.cloud_from(golden.patch_xyz, golden.patch_rgb)
+    assert ctx.L.gca3d_color_gradient(ctx.h, c.h, 0.05) == N.ERR_INVALID_VALUE
+
+
+# --------------------------------------------------------------------------- #
+# Gauss-Newton system for given correspondences
+# --------------------------------------------------------------------------- #
+def gn_f64(src, srgb, tx, trgb, tn, tg, nn, lam, orc):
+    m = nn >= 0
+    p = src[m].astype(np.float64)
+    j = nn[m]
+    q, n, d = tx[j].astype(np.float64), tn[j].astype(np.float64), tg[j].astype(np.float64)
+    Is = orc.intensity(srgb[m]).astype(np.float64)
+    It = orc.intensity(trgb[j]).astype(np.float64)
+    rg = ((p - q) * n).sum(1)
+    proj = p - rg[:, None] * n
+    rc = It + ((proj - q) * d).sum(1) - Is
+    dt = d - (n * d).sum(1)[:, None] * n
+    slg, slc = np.sqrt(np.float32(lam)).astype(np.float64), np.sqrt(np.float32(1) - np.float32(lam)).astype(np.float64)
+    Jg = slg * np.concatenate([np.cross(p, n), n], 1)
+    Jc = slc * np.concatenate([np.cross(p, dt), dt], 1)
+    A = Jg.T @ Jg + Jc.T @ Jc
+    b = Jg.T @ (slg * rg) + Jc.T @ (slc * rc)
+    r2 = ((slg * rg) ** 2 + (slc * rc) ** 2).sum()
+    return A, b, r2
+
+
+def test_build_gauss_newton(ctx, golden, orc):
+    tgt = ctx.cloud_from(golden.patch_xyz, golden.patch_rgb)
+    tgt.set_normals(golden["normals"])
+    tgt.set_gradients(golden["grad"])
+    src = ctx.cloud_from(golden["gn_src_xyz"], golden.gn_src_rgb)
+    nn = golden["gn_nn"]
+    buf = ctx.alloc(4 * len(nn))
+    buf.write(nn)
+    jtj, jtr, r2 = np.zeros(36), np.zeros(6), C.c_double()
+    ctx.check(ctx.L.gca3d_build_gauss_newton(ctx.h, src.h, tgt.h, buf.ptr, 0.968, jtj.ctypes.data, jtr.ctypes.data,
+                                             C.byref(r2)))
+    A, b, e = gn_f64(golden["gn_src_xyz"], golden.gn_src_rgb, golden.patch_xyz, golden.patch_rgb, golden["normals"],
+                     golden["grad"], nn, 0.968, orc)
+    scale = np.abs(A).max()
+    assert np.abs(jtj.reshape(6, 6) - A).max() < 1e-5 * scale
+    assert np.abs(jtr - b).max() < 1e-5 * np.abs(b).max()
+    assert abs(r2.value - e) < 1e-5 * e
+    # the reference's FP32 transform_reduce agrees to its own precision
+    assert np.abs(golden["gn_jtj"] - A).max() < 1e-3 * scale
+    res = ctx.alloc(4 * len(nn))
+    ctx.check(ctx.L.gca3d_abs_residual(ctx.h, src.h, tgt.h, buf.ptr, 0.968, res.ptr))
+    np.testing.assert_allclose(res.read(np.float32, len(nn)), golden["gn_abs_residual"], rtol=1e-4, atol=1e-6)
+
+
+def test_build_gauss_newton_rejects_bad_lambda(ctx, golden, N):
+    tgt = ctx.cloud_from(golden.patch_xyz, golden.patch_rgb)
+    src = ctx.cloud_from(golden["gn_src_xyz"])
+    buf = ctx.alloc(4 * 4000)
+    jtj, jtr = np.zeros(36), np.zeros(6)
+    assert ctx.L.gca3d_build_gauss_newton(ctx.h, src.h, tgt.h, buf.ptr, 1.5, jtj.ctypes.data, jtr.ctypes.data,
+                                          None) == N.ERR_INVALID_VALUE
+    assert ctx.L.gca3d_build_gauss_newton(ctx.h, src.h, tgt.h, buf.ptr, 0.9, jtj.ctypes.data, jtr.ctypes.data,
+                                          None) == N.ERR_INVALID_VALUE  # no normals / gradients
+
+
+# --------------------------------------------------------------------------- #
+# RGB-D frame -> cloud
+# --------------------------------------------------------------------------- #
+@pytest.fixture(scope="module")
+def frames():
+    from cuda_3d_gb300 import synth
+
+    return synth.frame_pair(seed=0)
+
+
+def frame_gpu(ctx, N, depth, bgr, mode, radius=2, ss=3.0, sd=30.0, tmin=0.2, tmax=10.0):
+    h, w = depth.shape
+    dbuf, cbuf = ctx.alloc(depth.nbytes), ctx.alloc(bgr.nbytes)
+    dbuf.write(depth)
+    cbuf.write(bgr)
+    out = ctx.cloud(h * w)
+    di = N.Intrinsics(525.0, 525.0, 319.5, 239.5)
+    f = N.Filter(mode, radius, ss, sd)
+    ctx.check(ctx.L.gca3d_frame_to_cloud(ctx.h, dbuf.ptr, cbuf.ptr, w, h, C.byref(di), None, None, 0.001, tmin, tmax,
+                                         C.byref(f), out.h))
+    return out.download()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_frame_to_cloud_vs_oracle(ctx, N, orc, frames, mode):
+    d = frame_gpu(ctx, N, frames.depth0, frames.bgr0, mode)
+    ox, oc = orc.make_point_cloud(frames.depth0, frames.bgr0, (525.0, 525.0, 319.5, 239.5), mode=mode, radius=2,
+                                  sigma_space=3.0, sigma_depth=30.0, tmin=0.2, tmax=10.0)
+    # bit-exact, raster order kept: the filter's exp is evaluated by the same
+    # operation sequence on both sides, so even the colour lookups, which sit on
+    # pixel boundaries for identity extrinsics, agree
+    np.testing.assert_array_equal(d["xyz"], ox)
+    np.testing.assert_array_equal(d["rgb"], oc)
+
+
+def test_frame_tmin_zero_nan_quirk(ctx, N, orc, frames):
+    """with tmin = 0 the reference turns isolated zero pixels into NaN points
+    (0 / 0 in the filter passes both threshold tests); the build keeps that"""
+    d = frame_gpu(ctx, N, frames.depth0, frames.bgr0, 1, tmin=0.0)
+    ox, _ = orc.make_point_cloud(frames.depth0, frames.bgr0, (525.0, 525.0, 319.5, 239.5), mode=1, tmin=0.0)
+    assert np.isnan(ox).any()
+    np.testing.assert_array_equal(d["xyz"], ox)

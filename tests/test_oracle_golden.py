@@ -119,3 +119,18 @@ def test_normals_f64_vs_reference(golden, orc):
     # zero normals exactly where fewer than 3 neighbours
     zero64 = np.linalg.norm(n64, axis=1) == 0
     np.testing.assert_array_equal(zero64, golden["radius_counts"] < 3)
+
+
+def test_filter_exp_error_bound(orc):
+    """the depth filter's exp (shared operation sequence with the CUDA kernel) is
+    within 2 ulp of exp(x) over the filter's argument range, subnormals included"""
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(-110, 90, 20000), rng.uniform(-3, 0.5, 20000)]).astype(np.float32)
+    y = orc.exp32(x).astype(np.float64)
+    t = np.exp(x.astype(np.float64))
+    normal = (t > np.finfo(np.float32).tiny) & (t < np.finfo(np.float32).max)
+    ulp = np.abs(y[normal] - t[normal]) / np.spacing(t[normal].astype(np.float32)).astype(np.float64)
+    assert ulp.max() <= 2.0
+    sub = t <= np.finfo(np.float32).tiny
+    assert np.all(np.abs(y[sub] - t[sub]) <= np.finfo(np.float32).smallest_subnormal)
+    assert orc.exp32([np.float32(100.0)])[0] == np.inf and orc.exp32([np.float32(-200.0)])[0] == 0.0
