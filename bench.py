@@ -1,0 +1,442 @@
+#!/usr/bin/env python
+"""Throughput of the colored-ICP registration path on GB300.
+
+Workload (default, "batch64"): 64 synthetic fragment pairs of uneven size (clouds
+log-uniform in 20k-300k points, per-pair rotation 0-15 deg, translation 0-15 cm,
+overlap 40-90 %), three-scale colored ICP (voxel 0.04/0.02/0.01 m, 50/30/14
+iterations, max correspondence 1.5 x voxel, normal and gradient radius 2 x voxel).
+A step registers the whole batch.  Metric: pairs/s (higher is better).
+
+  value  chosen path: one CUDA graph per batch (all pairs in every launch,
+         compensated FP32 accumulation, FP64 solve), inputs resident in HBM
+  e2e    the same through the C ABI with host buffers: per step the 128 clouds are
+         uploaded from pinned memory and the 64 results read back
+  plain  the one-pair-per-launch FP32 path: 64 sequential single-pair calls, eager
+         launches, convergence read back on the host after every iteration
+
+--impl reference times the reference's algorithm on the host cores (the CPU port
+in oracle/, FP32 in the reference's operation order, OpenMP) on the same workload.
+Multi-GPU (torchrun): every rank registers its own batch (weak scaling); no data
+moves between ranks, the barrier and the max-reduce of the step time are the only
+collectives.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# the schedule of the precision and batching workloads
+SCALES = [(0.04, 50, 0.06, 0.08, 0.08), (0.02, 30, 0.03, 0.04, 0.04), (0.01, 14, 0.015, 0.02, 0.02)]
+ICP_BYTES_PER_POINT = 16 + 48  # source xyz+I; target record: xyz+cell, normal+I, gradient
+ICP_BYTES_PER_BLOCK = 32 * 8   # one block partial (FP64)
+ICP_CHUNK = 1024
+
+
+def parse_args(argv=None):
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--pairs", type=int, default=64)
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--quick", action="store_true", help="value only (for profiler runs)")
+    return p.parse_args(argv)
+
+
+# --------------------------------------------------------------------------- #
+# ranks
+# --------------------------------------------------------------------------- #
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def dist_init(backend):
+    import torch.distributed as dist
+
+    rank, world, _ = dist_env()
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29511")
+        dist.init_process_group(backend, rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier():
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def reduce_max(x, device="cpu"):
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x, device="cpu"):
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def rank_seed(base, rank):
+    """each rank registers its own batch (weak scaling)"""
+    return base + 1009 * rank
+
+
+# --------------------------------------------------------------------------- #
+# clocks during the timed region
+# --------------------------------------------------------------------------- #
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        return self.summarise(rows)
+
+    @staticmethod
+    def summarise(rows):
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per ICP-iteration launch from the committed ncu capture, if any"""
+    path = os.path.join(ROOT, "profiles", "icp_iter_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+# --------------------------------------------------------------------------- #
+# workload
+# --------------------------------------------------------------------------- #
+def make_workload(n_pairs, seed):
+    from cuda_3d_gb300 import synth
+
+    sampler = synth.RoomSampler()
+    return synth.batch_pairs(n_pairs, seed=seed, sampler=sampler)
+
+
+def icp_algorithmic_bytes(results):
+    """compulsory HBM bytes of the ICP-iteration launches of one execute: per pair,
+    scale and iteration every source point reads its 16-byte xyzI and gathers its
+    48-byte target record (position, normal + intensity, gradient); each block
+    writes one 256-byte partial"""
+    total = 0
+    for r in results:
+        for s in range(len(SCALES)):
+            n, it = r["scale_n_src"][s], r["scale_iterations"][s]
+            total += it * (n * ICP_BYTES_PER_POINT + math.ceil(n / ICP_CHUNK) * ICP_BYTES_PER_BLOCK)
+    return total
+
+
+def pose_spread(a, b):
+    from cuda_3d_gb300 import synth
+
+    errs = [synth.pose_error(x["T"], y["T"]) for x, y in zip(a, b)]
+    return max(e[0] for e in errs), max(e[1] for e in errs)
+
+
+# --------------------------------------------------------------------------- #
+# our arm
+# --------------------------------------------------------------------------- #
+def run_ours(args):
+    import torch
+
+    from cuda_3d_gb300 import build, native as N
+    from cuda_3d_gb300 import synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist_init("nccl")
+    build.build()
+    # a dedicated stream: the library and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = N.Context(local, stream=stream.cuda_stream)
+    pairs = make_workload(args.pairs, rank_seed(args.seed, rank))
+    P = len(pairs)
+    n_src = sum(len(p.src_xyz) for p in pairs)
+    n_tgt = sum(len(p.tgt_xyz) for p in pairs)
+    srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
+    tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
+    scales = [N.scale(*s) for s in SCALES]
+    chosen = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True, use_graph=True)
+    plan = N.IcpPlan(ctx, srcs, tgts, chosen)
+    res_chosen = None
+    for _ in range(max(args.warmup, 3)):
+        res_chosen = plan.execute(results=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    # ---- value: resident inputs, graph replays -------------------------------
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        plan.execute(results=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier()
+    ms = reduce_max(ev0.elapsed_time(ev1) / args.steps, "cuda")
+    value = world * P / (ms / 1000.0)
+
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": "colored-ICP pairs/s (quick)", "value": value, "ms_per_step": ms,
+                              "gpu_launches": plan.kernels() * args.steps}))
+        return
+
+    # ---- e2e: host buffers through the C ABI ----------------------------------
+    host = []
+    for p in pairs:
+        bufs = []
+        for a in (p.src_xyz, p.src_rgb, p.tgt_xyz, p.tgt_rgb):
+            t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+            t.numpy()[:] = a
+            bufs.append(t)
+        host.append(bufs)
+    h2d = sum(b.numel() * 4 for bufs in host for b in bufs)
+    import ctypes as C
+
+    def upload_all():
+        for (sx, sc, tx, tc), s, t in zip(host, srcs, tgts):
+            ctx.check(ctx.L.gca3d_cloud_upload(ctx.h, s.h, C.c_void_p(sx.data_ptr()), C.c_void_p(sc.data_ptr()),
+                                               sx.shape[0]))
+            ctx.check(ctx.L.gca3d_cloud_upload(ctx.h, t.h, C.c_void_p(tx.data_ptr()), C.c_void_p(tc.data_ptr()),
+                                               tx.shape[0]))
+
+    for _ in range(2):
+        upload_all()
+        plan.execute(results=True)
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        upload_all()
+        res_e2e = plan.execute(results=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = reduce_max(ev0.elapsed_time(ev1) / args.steps, "cuda")
+    d2h = P * 184  # the pair states read back per step (sizeof PairState)
+    e2e = {"value": world * P / (ms_e2e / 1000.0), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e}
+
+    # ---- roofline of the ICP iteration kernel (eager run, CUDA events) ---------
+    prof = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True, use_graph=False)
+    plan_prof = N.IcpPlan(ctx, srcs, tgts, prof)
+    plan_prof.execute(results=True)
+    ctx.profile_begin("icp_iter")
+    res_prof = plan_prof.execute(results=True)
+    icp_ms, icp_launches = ctx.profile_read()
+    bytes_total = icp_algorithmic_bytes(res_prof)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_total / (icp_ms / 1e3) / 1e9
+    traffic = committed_traffic()
+    breakdown = {"icp_iter": {"ms": icp_ms, "launches": icp_launches}}
+    for k in ("sort_pass", "normals", "voxel_reduce", "grid_scatter"):
+        ctx.profile_begin(k)
+        plan_prof.execute(results=True)
+        t, n = ctx.profile_read()
+        breakdown[k] = {"ms": t, "launches": n}
+    roofline = {"kernel": "k_icp_iter (fused NN + residual + Jacobian + JTJ/JTr + FP64 solve)", "bound": "hbm",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                "algorithmic_bytes_per_launch": bytes_total / max(icp_launches, 1),
+                "avg_launch_us": icp_ms * 1e3 / max(icp_launches, 1), "launches": icp_launches}
+
+    # ---- plain: one pair per call, FP32, host convergence checks ----------------
+    plain = None
+    if not args.no_plain:
+        pp = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=False, use_graph=False)
+        res_plain = [N.color_icp(ctx, s, t, pp) for s, t in zip(srcs, tgts)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            res_plain = [N.color_icp(ctx, s, t, pp) for s, t in zip(srcs, tgts)]
+        torch.cuda.synchronize()
+        ms_plain = reduce_max((time.perf_counter() - t0) * 1e3 / reps, "cuda")
+        rot, tr = pose_spread(res_chosen, res_plain)
+        plain = {"value": world * P / (ms_plain / 1000.0), "unit": "pairs/s", "ms_per_step": ms_plain,
+                 "chosen_over_plain": (world * P / (ms / 1000.0)) / (world * P / (ms_plain / 1000.0)),
+                 "max_pose_diff_vs_chosen": {"rad": rot, "m": tr}}
+
+    gt = [synth.pose_error(r["T"], p.T_gt) for r, p in zip(res_chosen, pairs)]
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(pairs, sample=4)
+
+    line = {
+        "metric": "colored-ICP pairs/s (64-pair batch, three-scale)",
+        "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (FP64 solve and cross-block sums)", "data": "synthetic",
+        "config": {"workload": "batch64: 64 fragment pairs, clouds log-uniform 20k-300k points, rot 0-15 deg, "
+                               "trans 0-15 cm, overlap 40-90 %, scales voxel 0.04/0.02/0.01 m x 50/30/14 iterations",
+                   "pairs_per_gpu": P, "src_points": n_src, "tgt_points": n_tgt,
+                   "scales": SCALES, "parallelism": f"replicas x{world} (pairs sharded per rank)",
+                   "l2": f"inputs larger than L2 ({(n_src + n_tgt) * 32 / 1e6:.0f} MB resident SoA)"},
+        "e2e": e2e,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "plain": plain,
+        "kernel_breakdown_ms_per_execute": breakdown,
+        "gt_error_max": {"rad": max(g[0] for g in gt), "m": max(g[1] for g in gt)},
+        "gt_error_median": {"rad": statistics.median(g[0] for g in gt), "m": statistics.median(g[1] for g in gt)},
+        "clocks": clk,
+        "gpu_launches": plan.kernels() * args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+# --------------------------------------------------------------------------- #
+# CPU: the reference's algorithm on the host cores
+# --------------------------------------------------------------------------- #
+def cpu_baseline(pairs, sample=4):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    scales = [O.Scale(*s) for s in SCALES]
+    sub = pairs[:sample]
+    t0 = time.perf_counter()
+    for p in sub:
+        O.multiscale_ref32(p.src_xyz, p.src_rgb, p.tgt_xyz, p.tgt_rgb, scales)
+    dt = time.perf_counter() - t0
+    return {"value": len(sub) / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"pairs 0-{len(sub) - 1} of the batch, full three-scale schedule, "
+                      f"FP32 in the reference's operation order (oracle/gca_oracle.c), OpenMP"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    pairs = make_workload(args.pairs, rank_seed(args.seed, 0))
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    scales = [O.Scale(*s) for s in SCALES]
+    per_step = 2
+    k = 0
+
+    def step():
+        nonlocal k
+        for _ in range(per_step):
+            p = pairs[k % len(pairs)]
+            k += 1
+            O.multiscale_ref32(p.src_xyz, p.src_rgb, p.tgt_xyz, p.tgt_rgb, scales)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    value = per_step / dt
+    sample = (f"{per_step} pairs per step (cycling through the 64-pair batch), full three-scale schedule, "
+              f"FP32 in the reference's operation order (oracle/gca_oracle.c), OpenMP")
+    print(json.dumps({
+        "impl": "reference", "metric": "colored-ICP pairs/s (64-pair batch, three-scale)", "value": value,
+        "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batch64 (as the ours arm)", "pairs_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

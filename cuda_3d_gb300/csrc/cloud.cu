@@ -93,6 +93,21 @@ int consume_device_error(gca3d_context *ctx, const char *where)
     return GCA3D_OK;
 }
 
+void prof_mark(gca3d_context *ctx, int kid)
+{
+    Profiler &P = ctx->prof;
+    if (P.target != kid || kid == kKidNone)
+        return;
+    if (P.used == P.events.size())
+    {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess)
+            return;
+        P.events.push_back(e);
+    }
+    cudaEventRecord(P.events[P.used++], ctx->stream);
+}
+
 int ensure_attr(gca3d_context *ctx, gca3d_cloud *c, bool normals, bool grad)
 {
     size_t bytes = sizeof(float4) * (size_t)std::max<int64_t>(c->capacity, 1);
@@ -353,6 +368,8 @@ int gca3d_destroy(gca3d_context *ctx)
     if (ctx->stream)
         cudaStreamSynchronize(ctx->stream);
     ctx->arena.release();
+    for (auto e : ctx->prof.events)
+        cudaEventDestroy(e);
     if (ctx->d_err)
         cudaFree(ctx->d_err);
     if (ctx->h_pinned)
@@ -381,6 +398,39 @@ const char *gca3d_last_error(gca3d_context *ctx)
 int64_t gca3d_kernel_launches(gca3d_context *ctx) { return ctx ? ctx->launches : -1; }
 
 void *gca3d_stream(gca3d_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int gca3d_profile_begin(gca3d_context *ctx, const char *kernel)
+{
+    if (!ctx || !kernel)
+        return GCA3D_ERR_INVALID_VALUE;
+    static const char *names[kKidCount] = {"icp_iter", "sort_pass", "normals", "voxel_reduce", "grid_scatter",
+                                           "frame"};
+    ctx->prof.target = kKidNone;
+    for (int k = 0; k < kKidCount; ++k)
+        if (std::string(kernel) == names[k])
+            ctx->prof.target = k;
+    ctx->prof.used = 0;
+    return ctx->prof.target == kKidNone ? fail(ctx, GCA3D_ERR_INVALID_VALUE, "profile: unknown kernel") : GCA3D_OK;
+}
+
+int gca3d_profile_read(gca3d_context *ctx, double *total_ms, int64_t *launches)
+{
+    if (!ctx || !total_ms || !launches)
+        return GCA3D_ERR_INVALID_VALUE;
+    GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double t = 0.0;
+    for (size_t i = 0; i + 1 < ctx->prof.used; i += 2)
+    {
+        float ms = 0.0f;
+        GCA_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->prof.events[i], ctx->prof.events[i + 1]));
+        t += ms;
+    }
+    *total_ms = t;
+    *launches = (int64_t)(ctx->prof.used / 2);
+    ctx->prof.target = kKidNone;
+    ctx->prof.used = 0;
+    return GCA3D_OK;
+}
 
 int gca3d_device_alloc(gca3d_context *ctx, int64_t bytes, void **ptr)
 {

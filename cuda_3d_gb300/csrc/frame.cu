@@ -265,9 +265,11 @@ int frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr
     GCA_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(unsigned long long) * P.h, ctx->stream));
     const int R = P.mode == GCA3D_FILTER_FIXED ? P.radius : (P.mode == GCA3D_FILTER_ADAPTIVE ? 5 : 0);
     const size_t smem = (size_t)(2 * R + 1) * P.w * sizeof(uint16_t);
+    GCA_PROF_BEGIN(ctx, kKidFrame);
     k_frame<<<P.h, kFrameThreads, smem, ctx->stream>>>(depth, bgr, P, out->pos, out->col, out->d_count, tile_ctr,
                                                        status, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidFrame);
     return GCA3D_OK;
 }
 

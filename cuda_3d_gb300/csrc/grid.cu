@@ -219,8 +219,10 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     if (st)
         return st;
     const int gs = std::min(grid_for(cap), ctx->num_sms * 8);
+    GCA_PROF_BEGIN(ctx, kKidGridScatter);
     k_grid_scatter<<<gs, kBlock, 0, s>>>(sb, d_n, d.layout, b.pos, d.spos, d.sidx, d.sint, d.skey);
     GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidGridScatter);
     GCA_CUDA(ctx, cudaMemsetAsync(d.hkeys, 0xFF, sizeof(unsigned long long) * hcap, s));
     k_hash_insert<<<gs, kBlock, 0, s>>>(d.skey, d_n, d.layout, d.hkeys, d.hvals, d.hmask, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);

@@ -338,7 +338,7 @@ __device__ __forceinline__ int find_pair(const int *bmap, int P, int b)
 
 // per-scale setup: block map, per-pair counts, reset of the per-scale flags
 __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-                            int chunk, int first_scale)
+                            int chunk, int scale)
 {
     if (threadIdx.x != 0)
         return;
@@ -357,11 +357,16 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
         S.ticket = 0;
         S.active = nb > 0 ? 1 : 0;
         S.converged = 0;
-        if (first_scale)
+        if (scale == 0)
         {
             S.iters = 0;
             S.status = 0;
+            for (int k = 0; k < GCA3D_MAX_SCALES; ++k)
+                S.scale_iters[k] = S.scale_nsrc[k] = S.scale_ntgt[k] = 0;
         }
+        S.scale = scale;
+        S.scale_nsrc[scale] = ns;
+        S.scale_ntgt[scale] = nt;
         if (nb == 0)
         {
             S.status = GCA3D_ERR_NO_CORRESPONDENCES;
@@ -505,6 +510,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_iter(const float4 *__restri
         for (int k = 0; k < 16; ++k)
             Ps.T[k] = Tn[k];
         Ps.iters += 1;
+        Ps.scale_iters[Ps.scale] += 1;
         // convergence test of color_icp.cu:216-228 on this step
         const double cth = 0.5 * (Ti[0] + Ti[5] + Ti[10] - 1.0);
         const double tsq = Ti[3] * Ti[3] + Ti[7] * Ti[7] + Ti[11] * Ti[11];
@@ -518,9 +524,9 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_iter(const float4 *__restri
 }
 
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-              bool first_scale)
+              int scale)
 {
-    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, kIcpChunk, first_scale ? 1 : 0);
+    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, kIcpChunk, scale);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
@@ -536,6 +542,7 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
                   PairState *st, const int *bmap, int max_blocks, double *partials, const IcpScale &prm,
                   bool compensated, int32_t *nn_out)
 {
+    GCA_PROF_BEGIN(ctx, kKidIcpIter);
     if (compensated)
         k_icp_iter<true><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, attr0, attr1, st,
                                                                       bmap, src.P, partials, prm, nn_out);
@@ -543,6 +550,7 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
         k_icp_iter<false><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, attr0, attr1, st,
                                                                        bmap, src.P, partials, prm, nn_out);
     GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidIcpIter);
     return GCA3D_OK;
 }
 

@@ -23,6 +23,10 @@ struct PairState
     int nblocks;
     int nsrc;
     int ntgt;
+    int scale;
+    int scale_iters[GCA3D_MAX_SCALES];
+    int scale_nsrc[GCA3D_MAX_SCALES];
+    int scale_ntgt[GCA3D_MAX_SCALES];
 };
 
 struct IcpScale
@@ -35,7 +39,7 @@ struct IcpScale
 
 int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit);
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-              bool first_scale);
+              int scale);
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, const int *bmap, int max_blocks, double *partials, const IcpScale &prm,
                   bool compensated, int32_t *nn_out);

@@ -75,6 +75,27 @@ struct Arena
 // ---------------------------------------------------------------------------
 // opaque handles
 // ---------------------------------------------------------------------------
+namespace gca3d
+{
+enum KernelId : int
+{
+    kKidNone = -1,
+    kKidIcpIter = 0,
+    kKidSortPass,
+    kKidNormals,
+    kKidVoxelReduce,
+    kKidGridScatter,
+    kKidFrame,
+    kKidCount
+};
+struct Profiler
+{
+    int target = kKidNone;
+    std::vector<cudaEvent_t> events; // start/stop pairs
+    size_t used = 0;
+};
+} // namespace gca3d
+
 struct gca3d_context
 {
     int device = 0;
@@ -86,6 +107,7 @@ struct gca3d_context
     int *h_pinned = nullptr; // pinned scratch for small read-backs (64 ints)
     int64_t launches = 0;
     std::string last_error;
+    gca3d::Profiler prof;
 };
 
 struct gca3d_cloud
@@ -125,6 +147,11 @@ int cuda_fail(gca3d_context *ctx, cudaError_t e, const char *where);
         if (e_ != cudaSuccess)                                                                     \
             return ::gca3d::cuda_fail((ctx), e_, __func__);                                        \
     } while (0)
+
+// event bracket around launches of the profiled kernel (no-op otherwise)
+void prof_mark(gca3d_context *ctx, int kid);
+#define GCA_PROF_BEGIN(ctx, kid) ::gca3d::prof_mark((ctx), (kid))
+#define GCA_PROF_END(ctx, kid) ::gca3d::prof_mark((ctx), (kid))
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 inline int grid_for(int64_t n, int per_block = kBlock)

@@ -348,9 +348,11 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
     if (!do_normals && !in_nrm)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gradient: normals needed");
     const int gs = std::min(grid_for(g.cap), ctx->num_sms * 8);
+    GCA_PROF_BEGIN(ctx, kKidNormals);
     k_normals_grad<<<gs, 256, 0, ctx->stream>>>(g.dev, b.seg_off + b.P, do_normals ? 1 : 0, normal_radius, max_nn,
                                                 do_grad ? 1 : 0, grad_radius, in_nrm, attr0, attr1, nrm_out, grd_out);
     GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidNormals);
     return GCA3D_OK;
 }
 

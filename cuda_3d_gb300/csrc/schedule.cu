@@ -126,7 +126,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
                                 keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
             return st;
-        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, si == 0)))
+        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, si)))
             return st;
         IcpScale prm;
         prm.max_corr = S.max_corr;
@@ -184,6 +184,12 @@ void fill_results(const gca3d_icp_plan *pl, gca3d_icp_result *res)
         r.status = S.status;
         r.n_src = S.nsrc;
         r.n_tgt = S.ntgt;
+        for (int k = 0; k < GCA3D_MAX_SCALES; ++k)
+        {
+            r.scale_iterations[k] = S.scale_iters[k];
+            r.scale_n_src[k] = S.scale_nsrc[k];
+            r.scale_n_tgt[k] = S.scale_ntgt[k];
+        }
     }
 }
 

@@ -305,10 +305,12 @@ int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t 
     GCA_CHECK_LAUNCH(ctx);
     for (int p = 0; p < npasses; ++p)
     {
+        GCA_PROF_BEGIN(ctx, kKidSortPass);
         k_sort_pass<<<(int)(ntiles > 0 ? ntiles : 1), kSortThreads, 0, ctx->stream>>>(
             sb.keys[0], sb.vals[0], sb.keys[1], sb.vals[1], ctl, status + (p & 1) * status_words,
             status + ((p + 1) & 1) * status_words, status_words, p, d_n, ctx->d_err);
         GCA_CHECK_LAUNCH(ctx);
+        GCA_PROF_END(ctx, kKidSortPass);
     }
     return GCA3D_OK;
 }

@@ -298,9 +298,11 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts);
     GCA_CHECK_LAUNCH(ctx);
     GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0, sizeof(int32_t) * P, s));
+    GCA_PROF_BEGIN(ctx, kKidVoxelReduce);
     k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col,
                                          seg_count);
     GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidVoxelReduce);
     k_counts_to_offsets<<<1, 32, 0, s>>>(seg_count, P, out.seg_off);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;

@@ -56,7 +56,9 @@ class IcpParams(C.Structure):
 class IcpResult(C.Structure):
     _fields_ = [("T", C.c_double * 16), ("rmse_ref", C.c_double), ("fitness", C.c_double),
                 ("inlier_rmse", C.c_double), ("iterations", C.c_int), ("converged", C.c_int),
-                ("status", C.c_int), ("n_src", C.c_int), ("n_tgt", C.c_int)]
+                ("status", C.c_int), ("n_src", C.c_int), ("n_tgt", C.c_int),
+                ("scale_iterations", C.c_int * MAX_SCALES), ("scale_n_src", C.c_int * MAX_SCALES),
+                ("scale_n_tgt", C.c_int * MAX_SCALES)]
 
 
 _P = C.c_void_p
@@ -70,6 +72,8 @@ _SIGS = {
     "gca3d_last_error": [_P],
     "gca3d_kernel_launches": [_P],
     "gca3d_stream": [_P],
+    "gca3d_profile_begin": [_P, C.c_char_p],
+    "gca3d_profile_read": [_P, C.POINTER(C.c_double), C.POINTER(_I64)],
     "gca3d_device_alloc": [_P, _I64, C.POINTER(_P)],
     "gca3d_device_free": [_P, _P],
     "gca3d_copy": [_P, _P, _P, _I64],
@@ -176,6 +180,14 @@ class Context:
 
     def launches(self):
         return self.L.gca3d_kernel_launches(self.h)
+
+    def profile_begin(self, kernel):
+        self.check(self.L.gca3d_profile_begin(self.h, kernel.encode()))
+
+    def profile_read(self):
+        ms, n = C.c_double(), C.c_int64()
+        self.check(self.L.gca3d_profile_read(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     # -- buffers ---------------------------------------------------------
     def alloc(self, nbytes):
@@ -288,7 +300,8 @@ def icp_params(scales, lam=0.968, update_map=UPDATE_EULER_ZYX, rot_eps=1e-6, tra
 def result_dict(r):
     return dict(T=np.array(r.T[:]).reshape(4, 4), rmse_ref=r.rmse_ref, fitness=r.fitness,
                 inlier_rmse=r.inlier_rmse, iterations=r.iterations, converged=bool(r.converged),
-                status=r.status, n_src=r.n_src, n_tgt=r.n_tgt)
+                status=r.status, n_src=r.n_src, n_tgt=r.n_tgt, scale_iterations=list(r.scale_iterations),
+                scale_n_src=list(r.scale_n_src), scale_n_tgt=list(r.scale_n_tgt))
 
 
 def cloud_array(clouds):

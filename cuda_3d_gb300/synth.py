@@ -223,15 +223,50 @@ def room_pair(seed, n_points=250_000, overlap=0.6, rot_deg=10.0, trans=0.10, sce
     return Pair(src, scol, tgt.astype(np.float32), tcol, T_gt)
 
 
-def batch_pairs(n_pairs=64, seed=0, n_min=20_000, n_max=300_000, max_rot=15.0, max_trans=0.15):
-    """the multi-pair workload: log-uniform sizes, per-pair transform and overlap"""
+class RoomSampler:
+    """a large clean area-uniform sample of the room (with colours) that many pairs
+    draw from; each draw adds fresh position noise"""
+
+    def __init__(self, scene_seed=1234, n_master=2_000_000, seed=99):
+        rng = np.random.default_rng(seed)
+        self.scene = room_scene(scene_seed)
+        self.xyz, self.rgb = sample_room(self.scene, n_master, rng, noise_sigma=0.0)
+
+    def draw(self, rng, n, noise_sigma=0.003):
+        idx = rng.integers(0, len(self.xyz), n)
+        return (self.xyz[idx] + rng.normal(scale=noise_sigma, size=(n, 3))).astype(np.float32), self.rgb[idx]
+
+
+def room_pair_from(sampler, seed, n_points, overlap=0.6, rot_deg=10.0, trans=0.10):
+    """room_pair with both views drawn from a shared RoomSampler"""
+    rng = np.random.default_rng(seed)
+    ang = rng.uniform(0, 2 * math.pi)
+    d = np.array([math.cos(ang), math.sin(ang)])
+    half = 0.5 * (abs(d[0]) * ROOM[0] + abs(d[1]) * ROOM[1])
+    s = 2 * half / (2 - overlap)
+    m = int(n_points * 2 * half / s) + 1
+    tgt, tcol = _crop(*sampler.draw(rng, m), d, half - s, half)
+    src, scol = _crop(*sampler.draw(rng, m), d, -half, -half + s)
+    tgt, tcol, src, scol = tgt[:n_points], tcol[:n_points], src[:n_points], scol[:n_points]
+    R = random_rotation(rng, rot_deg)
+    tdir = rng.normal(size=3)
+    t = tdir / np.linalg.norm(tdir) * trans
+    c = np.array([ROOM[0] / 2, ROOM[1] / 2, ROOM[2] / 2])
+    T_gt = make_T(R, c + t - R @ c)
+    return Pair(transform(np.linalg.inv(T_gt), src), scol, tgt.astype(np.float32), tcol, T_gt)
+
+
+def batch_pairs(n_pairs=64, seed=0, n_min=20_000, n_max=300_000, max_rot=15.0, max_trans=0.15, sampler=None):
+    """the multi-pair workload: sizes log-uniform in [n_min, n_max] per cloud, a
+    random transform per pair (rotation uniform in [0, max_rot] deg about a random
+    axis, translation uniform in [0, max_trans] m) and overlap uniform in [0.4, 0.9]"""
+    sampler = sampler or RoomSampler()
     out = []
     for k in range(n_pairs):
         rng = np.random.default_rng(10_000 + seed * 1000 + k)
         n = int(math.exp(rng.uniform(math.log(n_min), math.log(n_max))))
-        out.append(room_pair(seed=7 * k + 1 + seed * 100_003, n_points=n,
-                             overlap=rng.uniform(0.4, 0.9), rot_deg=rng.uniform(0, max_rot),
-                             trans=rng.uniform(0, max_trans)))
+        out.append(room_pair_from(sampler, 7 * k + 1 + seed * 100_003, n, overlap=rng.uniform(0.4, 0.9),
+                                  rot_deg=rng.uniform(0, max_rot), trans=rng.uniform(0, max_trans)))
     return out
 
 

@@ -103,6 +103,9 @@ typedef struct {
     int status;         /* GCA3D_OK, NO_CORRESPONDENCES, SINGULAR, TIMEOUT */
     int n_src;          /* source points at the last scale */
     int n_tgt;          /* target points at the last scale */
+    int scale_iterations[GCA3D_MAX_SCALES]; /* per scale */
+    int scale_n_src[GCA3D_MAX_SCALES];
+    int scale_n_tgt[GCA3D_MAX_SCALES];
 } gca3d_icp_result;
 
 /* ---------------------------------------------------------------------------
@@ -118,6 +121,11 @@ const char *gca3d_status_string(int status);
 const char *gca3d_last_error(gca3d_context *ctx);
 /* number of kernels this library launched on the context since creation */
 int64_t gca3d_kernel_launches(gca3d_context *ctx);
+/* kernel timing with CUDA events on the context stream: while a profile is open,
+ * every launch of the named kernel ("icp_iter", "sort_pass", "normals", "voxel_reduce",
+ * "grid_scatter", "frame") is bracketed by events; read sums their durations */
+int gca3d_profile_begin(gca3d_context *ctx, const char *kernel);
+int gca3d_profile_read(gca3d_context *ctx, double *total_ms, int64_t *launches);
 /* the context's stream (cudaStream_t) */
 void *gca3d_stream(gca3d_context *ctx);
 /* plain device buffers for callers without their own allocator */
