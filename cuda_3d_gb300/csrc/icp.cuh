@@ -37,6 +37,13 @@ struct IcpScale
     double rot_eps, trans_eps;
 };
 
+// the Gauss-Newton system for given correspondences (defined in icp.cu); the block
+// partials, the ticket and the count are scratch supplied by the caller
+__global__ void __launch_bounds__(kIcpThreads)
+    k_build_gn(const float4 *__restrict__ sp, const int32_t *d_ns, const float4 *__restrict__ tp,
+               const float4 *__restrict__ tn, const float4 *__restrict__ tg, const int32_t *nn, float slg, float slc,
+               double *partials, unsigned *ticket, double *out);
+
 int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit);
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
               int scale);

@@ -99,6 +99,7 @@ _SIGS = {
     "gca3d_nn_search": [_P, _P, _P, _F, _P],
     "gca3d_radius_search": [_P, _P, _P, _F, _P, _P, _P, _P, _I64, C.POINTER(_I64)],
     "gca3d_build_gauss_newton": [_P, _P, _P, _P, _F, _P, _P, C.POINTER(C.c_double)],
+    "gca3d_build_gauss_newton_static": [_P, _P, C.c_int32, _P, _P, _P, _P, _F, _P, _P, _P],
     "gca3d_abs_residual": [_P, _P, _P, _P, _F, _P],
     "gca3d_color_icp": [_P, _P, _P, C.POINTER(IcpParams), _P, C.POINTER(IcpResult)],
     "gca3d_color_icp_batched": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), _P, _P],

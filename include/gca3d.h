@@ -220,6 +220,27 @@ int gca3d_build_gauss_newton(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *
                              const int32_t *nn, float lambda, double jtj[36], double jtr[6],
                              double *r2);
 
+/* The same system as gca3d_build_gauss_newton for callers that cannot allocate device
+ * memory while they run (a real-time loop that must not stall on cudaMalloc's device
+ * synchronisation, or a host whose memory manager already owns the GPU's memory).  No
+ * counterpart in the reference.  It needs no context and allocates nothing: inputs and
+ * outputs are the caller's device pointers, and the scratch (block partials, count,
+ * ticket) is a fixed 512 KiB array inside the library that every GPU loading the
+ * library holds until exit.
+ *   stream   cudaStream_t (NULL: the legacy default stream)
+ *   src_pos  device float4[n_src] {x, y, z, intensity} (the cloud layout above)
+ *   tgt_pos, tgt_nrm, tgt_grd  device float4 arrays of the target (layout above)
+ *   nn       device int32[n_src], target index or -1
+ *   jtj, jtr, r2  device double[36], double[6], double[1] outputs
+ * n_src above 8,388,608 returns GCA3D_ERR_CAPACITY.  The first call on each device
+ * looks up the scratch array's device address (cudaGetSymbolAddress); make that first
+ * call before any stream capture.  Every call uses the same array: calls that overlap
+ * on the GPU (other streams, other threads) race and must be serialised by the caller. */
+int gca3d_build_gauss_newton_static(void *stream, const void *src_pos, int32_t n_src,
+                                    const void *tgt_pos, const void *tgt_nrm,
+                                    const void *tgt_grd, const int32_t *nn, float lambda,
+                                    double *jtj, double *jtr, double *r2);
+
 /* |r_geometric| + |r_colour| per source point (device float[n_src]).
  * reference: cuda_compute_abs_residual_color_icp
  * (src/registration/cuda_color_icp_build_least_square.cu:310-350) */
