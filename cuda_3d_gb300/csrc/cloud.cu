@@ -164,6 +164,8 @@ __global__ void k_bounds(const float4 *__restrict__ pos, const int32_t *seg_off,
 {
     const int seg = blockIdx.y;
     const int b = seg_off[seg], e = seg_off[seg + 1];
+    if (b + (int64_t)blockIdx.x * blockDim.x >= e)
+        return;
     float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x)
     {
@@ -171,24 +173,7 @@ __global__ void k_bounds(const float4 *__restrict__ pos, const int32_t *seg_off,
         mn[0] = fminf(mn[0], p.x), mn[1] = fminf(mn[1], p.y), mn[2] = fminf(mn[2], p.z);
         mx[0] = fmaxf(mx[0], p.x), mx[1] = fmaxf(mx[1], p.y), mx[2] = fmaxf(mx[2], p.z);
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-    {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-        }
-    }
-    if ((threadIdx.x & 31) == 0 && b < e)
-    {
-        for (int a = 0; a < 3; ++a)
-        {
-            atomicMin(ord + 6 * seg + a, float_to_ordered(mn[a]));
-            atomicMax(ord + 6 * seg + 3 + a, float_to_ordered(mx[a]));
-        }
-    }
+    block_bounds_commit(mn, mx, ord + 6 * seg);
 }
 
 // single-segment offsets {0, n} from a device count

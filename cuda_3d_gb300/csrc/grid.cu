@@ -96,7 +96,7 @@ __global__ void k_grid_keys(const float4 *__restrict__ pos, const int32_t *seg_o
 }
 
 __global__ void k_grid_scatter(SortBuffers sb, const int32_t *d_n, const KeyLayout *lay, const float4 *__restrict__ pos,
-                               float4 *spos, int32_t *sidx, float *sint, uint64_t *skey)
+                               float4 *spos, int32_t *sidx, float *sint, int *scz, uint64_t *skey)
 {
     const int n = *d_n;
     const uint64_t *keys = sb.keys[*sb.d_sel];
@@ -111,28 +111,33 @@ __global__ void k_grid_scatter(SortBuffers sb, const int32_t *d_n, const KeyLayo
         spos[s] = make_float4(p.x, p.y, p.z, __int_as_float((int)(k & mz)));
         sidx[s] = g;
         sint[s] = p.w;
+        scz[s] = (int)(k & mz);
         skey[s] = k;
     }
 }
 
-__global__ void k_hash_insert(const uint64_t *skey, const int32_t *d_n, const KeyLayout *lay,
-                              unsigned long long *hkeys, int2 *hvals, uint32_t hmask, int *d_err)
+__global__ void k_hash_insert(const uint64_t *skey, const int32_t *d_n, const KeyLayout *lay, RowSlot *slots,
+                              uint32_t hmask, int *d_err)
 {
     const int n = *d_n;
     const int bz = lay->bz;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
-        unsigned long long rk = skey[s] >> bz;
+        const unsigned long long rk = skey[s] >> bz;
         if (s > 0 && (skey[s - 1] >> bz) == rk)
             continue;
+        int e = s + 1;
+        while (e < n && (skey[e] >> bz) == rk)
+            ++e;
         uint32_t h = hash_u64(rk) & hmask;
         bool done = false;
         for (uint32_t probe = 0; probe <= hmask; ++probe)
         {
-            unsigned long long prev = atomicCAS(hkeys + h, kEmptyKey, rk);
+            const unsigned long long prev = atomicCAS(&slots[h].key, kEmptyKey, rk);
             if (prev == kEmptyKey || prev == rk)
             {
-                hvals[h].x = s;
+                slots[h].start = s;
+                slots[h].end = e;
                 done = true;
                 break;
             }
@@ -140,29 +145,6 @@ __global__ void k_hash_insert(const uint64_t *skey, const int32_t *d_n, const Ke
         }
         if (!done)
             atomicOr(d_err, kErrCapacity);
-    }
-}
-
-__global__ void k_hash_end(const uint64_t *skey, const int32_t *d_n, const KeyLayout *lay,
-                           const unsigned long long *hkeys, int2 *hvals, uint32_t hmask)
-{
-    const int n = *d_n;
-    const int bz = lay->bz;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
-    {
-        unsigned long long rk = skey[s] >> bz;
-        if (s + 1 < n && (skey[s + 1] >> bz) == rk)
-            continue;
-        uint32_t h = hash_u64(rk) & hmask;
-        for (uint32_t probe = 0; probe <= hmask; ++probe)
-        {
-            if (hkeys[h] == rk)
-            {
-                hvals[h].y = s + 1;
-                break;
-            }
-            h = (h + 1) & hmask;
-        }
     }
 }
 
@@ -189,9 +171,9 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     d.spos = A.get<float4>(cap);
     d.sidx = A.get<int32_t>(cap);
     d.sint = A.get<float>(cap);
+    d.scz = A.get<int>(cap);
     d.skey = A.get<uint64_t>(cap);
-    d.hkeys = A.get<unsigned long long>(hcap);
-    d.hvals = A.get<int2>(hcap);
+    d.slots = A.get<RowSlot>(hcap);
     d.hmask = hcap - 1;
     d.seg_off = b.seg_off;
     int *ord = A.get<int>(6 * P);
@@ -201,7 +183,7 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     sb.vals[0] = A.get<int32_t>(cap);
     sb.vals[1] = A.get<int32_t>(cap);
     sb.d_sel = A.get<int>(1);
-    if (!d.gmin || !d.layout || !d.spos || !d.sidx || !d.sint || !d.skey || !d.hkeys || !d.hvals || !ord || !sb.keys[1] ||
+    if (!d.gmin || !d.layout || !d.spos || !d.sidx || !d.sint || !d.scz || !d.skey || !d.slots || !ord || !sb.keys[1] ||
         !sb.vals[1] || !sb.d_sel)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "grid_build: scratch");
     cudaStream_t s = ctx->stream;
@@ -220,13 +202,11 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
         return st;
     const int gs = std::min(grid_for(cap), ctx->num_sms * 8);
     GCA_PROF_BEGIN(ctx, kKidGridScatter);
-    k_grid_scatter<<<gs, kBlock, 0, s>>>(sb, d_n, d.layout, b.pos, d.spos, d.sidx, d.sint, d.skey);
+    k_grid_scatter<<<gs, kBlock, 0, s>>>(sb, d_n, d.layout, b.pos, d.spos, d.sidx, d.sint, d.scz, d.skey);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidGridScatter);
-    GCA_CUDA(ctx, cudaMemsetAsync(d.hkeys, 0xFF, sizeof(unsigned long long) * hcap, s));
-    k_hash_insert<<<gs, kBlock, 0, s>>>(d.skey, d_n, d.layout, d.hkeys, d.hvals, d.hmask, ctx->d_err);
-    GCA_CHECK_LAUNCH(ctx);
-    k_hash_end<<<gs, kBlock, 0, s>>>(d.skey, d_n, d.layout, d.hkeys, d.hvals, d.hmask);
+    GCA_CUDA(ctx, cudaMemsetAsync(d.slots, 0xFF, sizeof(RowSlot) * hcap, s));
+    k_hash_insert<<<gs, kBlock, 0, s>>>(d.skey, d_n, d.layout, d.slots, d.hmask, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
@@ -240,11 +220,15 @@ __global__ void k_nn_query(const float4 *__restrict__ q, const int32_t *d_nq, Gr
     const KeyLayout L = *g.layout;
     const float3 o = g.gmin[0];
     const float rr = __fmul_rn(radius, radius);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x)
+    const int per_block = blockDim.x / kSub;
+    for (int base = blockIdx.x * per_block; base < nq; base += gridDim.x * per_block)
     {
-        float4 p = q[i];
-        NNBest best = nn_search_one(g, L, 0, o, make_float3(p.x, p.y, p.z), rr);
-        out[i] = best.t >= 0 ? g.sidx[best.t] : -1;
+        const int i = base + (int)(threadIdx.x / kSub);
+        const bool valid = i < nq;
+        const float4 p = q[valid ? i : 0];
+        const NNBest best = nn_search_sub(g, L, 0, o, make_float3(p.x, p.y, p.z), rr, valid);
+        if (valid && (threadIdx.x & (kSub - 1)) == 0)
+            out[i] = best.t >= 0 ? g.sidx[best.t] : -1;
     }
 }
 
@@ -294,7 +278,7 @@ __global__ void k_radius_fill(const float4 *__restrict__ q, const int32_t *d_nq,
 int nn_query(gca3d_context *ctx, const float4 *qpos, const int32_t *d_nq, int64_t qcap, const Grid &g, float radius,
              int32_t *out_idx)
 {
-    const int gs = std::min(grid_for(qcap), ctx->num_sms * 16);
+    const int gs = std::min(grid_for(qcap, kBlock / kSub), ctx->num_sms * 16);
     k_nn_query<<<gs, kBlock, 0, ctx->stream>>>(qpos, d_nq, g.dev, radius, out_idx);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;

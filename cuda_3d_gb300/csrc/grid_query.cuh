@@ -6,59 +6,96 @@
 namespace gca3d
 {
 
-// visit the grid points of the 27 cells around p in the reference's scan order
-// (x offset, then y offset, then z, then ascending original index; the order of
-// nn_search_functor, src/geometry/cuda_nn_search.cu:164-206).  f(t, spos[t]).
-template <class F>
-__device__ __forceinline__ void grid_visit(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p, F &&f)
+// the 9 rows (x offset, then y offset) around a point: [start, end) in the sorted
+// arrays, and the z-cell window [lo, hi]
+struct GridRows
+{
+    int2 r[9];
+    int lo, hi;
+};
+
+// Probe all 9 rows with independent 16-byte loads (one round of memory latency for
+// the common case where the first slot answers), then resolve the rare collisions.
+// Returns false when p lies outside the grid's key range.
+__device__ __forceinline__ bool grid_rows(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p,
+                                          GridRows &R)
 {
     const int cx = cell_of(p.x, o.x, g.cell), cy = cell_of(p.y, o.y, g.cell), cz = cell_of(p.z, o.z, g.cell);
     const int mx = (1 << L.bx) - 1, my = (1 << L.by) - 1, mz = (1 << L.bz) - 1;
     if (cx < -1 || cx > mx + 1 || cy < -1 || cy > my + 1 || cz < -1 || cz > mz + 1)
-        return;
+        return false;
     const unsigned long long segbits = (unsigned long long)seg << (L.bx + L.by);
-    const int lo = cz - 1, hi = cz + 1;
-    for (int dx = -1; dx <= 1; ++dx)
+    unsigned long long rk[9];
+    uint32_t h[9];
+    ulonglong2 v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
     {
-        const int x = cx + dx;
-        if (x < 0 || x > mx)
+        const int x = cx + k / 3 - 1, y = cy + k % 3 - 1;
+        const bool ok = x >= 0 && x <= mx && y >= 0 && y <= my;
+        rk[k] = ok ? (segbits | ((unsigned long long)x << L.by) | (unsigned long long)y) : kEmptyKey;
+        h[k] = hash_u64(rk[k]) & g.hmask;
+        v[k] = ok ? slot_load(g.slots, h[k]) : make_ulonglong2(kEmptyKey, 0ull);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+    {
+        if (rk[k] != kEmptyKey && v[k].x == rk[k])
+            R.r[k] = make_int2((int)(uint32_t)v[k].y, (int)(uint32_t)(v[k].y >> 32));
+        else if (rk[k] != kEmptyKey && v[k].x != kEmptyKey)
+            R.r[k] = row_probe_rest(g.slots, g.hmask, rk[k], h[k]);
+        else
+            R.r[k] = make_int2(0, 0);
+    }
+    R.lo = cz - 1;
+    R.hi = cz + 1;
+    return true;
+}
+
+// visit the points of the probed rows whose z cell lies in [lo, hi], in the
+// reference's scan order (x offset, then y offset, then z, then ascending original
+// index; nn_search_functor, src/geometry/cuda_nn_search.cu:164-206).  f(t, spos[t]).
+template <class F> __device__ __forceinline__ void grid_scan(const GridDev &g, const GridRows &R, F &&f)
+{
+#pragma unroll
+    for (int k = 0; k < 9; ++k)
+    {
+        int t = R.r[k].x;
+        const int e = R.r[k].y;
+        if (t >= e)
             continue;
-        for (int dy = -1; dy <= 1; ++dy)
+        if (e - t > 16)
         {
-            const int y = cy + dy;
-            if (y < 0 || y > my)
-                continue;
-            const unsigned long long rk = segbits | ((unsigned long long)x << L.by) | (unsigned long long)y;
-            const int2 r = row_lookup(g.hkeys, g.hvals, g.hmask, rk);
-            int t = r.x;
-            const int e = r.y;
-            if (t >= e)
-                continue;
-            if (e - t > 16)
+            int a = t, b = e;
+            while (a < b)
             {
-                int a = t, b = e;
-                while (a < b)
-                {
-                    int m = (a + b) >> 1;
-                    if (__float_as_int(__ldg(&g.spos[m].w)) < lo)
-                        a = m + 1;
-                    else
-                        b = m;
-                }
-                t = a;
+                const int m = (a + b) >> 1;
+                if (__ldg(&g.scz[m]) < R.lo)
+                    a = m + 1;
+                else
+                    b = m;
             }
-            for (; t < e; ++t)
-            {
-                const float4 q = __ldg(&g.spos[t]);
-                const int qz = __float_as_int(q.w);
-                if (qz < lo)
-                    continue;
-                if (qz > hi)
-                    break;
-                f(t, q);
-            }
+            t = a;
+        }
+        for (; t < e; ++t)
+        {
+            const float4 q = __ldg(&g.spos[t]);
+            const int qz = __float_as_int(q.w);
+            if (qz < R.lo)
+                continue;
+            if (qz > R.hi)
+                break;
+            f(t, q);
         }
     }
+}
+
+template <class F>
+__device__ __forceinline__ void grid_visit(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p, F &&f)
+{
+    GridRows R;
+    if (grid_rows(g, L, seg, o, p, R))
+        grid_scan(g, R, f);
 }
 
 struct NNBest
@@ -80,6 +117,121 @@ __device__ __forceinline__ NNBest nn_search_one(const GridDev &g, const KeyLayou
             b.t = t;
         }
     });
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+// 4 lanes per query: lane `sub` of a 4-lane group probes and scans rows
+// sub, sub + 4, sub + 8 of the 9, so the dependent chain of a query is a third
+// as long; the group combines its partial results with width-4 shuffles.
+// ---------------------------------------------------------------------------
+constexpr int kSub = 4;
+
+struct SubRows
+{
+    int2 r[3];
+    int lo, hi;
+};
+
+__device__ __forceinline__ bool grid_rows_sub(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p,
+                                              int sub, SubRows &R)
+{
+    const int cx = cell_of(p.x, o.x, g.cell), cy = cell_of(p.y, o.y, g.cell), cz = cell_of(p.z, o.z, g.cell);
+    const int mx = (1 << L.bx) - 1, my = (1 << L.by) - 1, mz = (1 << L.bz) - 1;
+    R.r[0] = R.r[1] = R.r[2] = make_int2(0, 0);
+    if (cx < -1 || cx > mx + 1 || cy < -1 || cy > my + 1 || cz < -1 || cz > mz + 1)
+        return false;
+    const unsigned long long segbits = (unsigned long long)seg << (L.bx + L.by);
+    unsigned long long rk[3];
+    uint32_t h[3];
+    ulonglong2 v[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+    {
+        const int k = sub + kSub * j;
+        const int x = cx + k / 3 - 1, y = cy + k % 3 - 1;
+        const bool ok = k < 9 && x >= 0 && x <= mx && y >= 0 && y <= my;
+        rk[j] = ok ? (segbits | ((unsigned long long)x << L.by) | (unsigned long long)y) : kEmptyKey;
+        h[j] = hash_u64(rk[j]) & g.hmask;
+        v[j] = ok ? slot_load(g.slots, h[j]) : make_ulonglong2(kEmptyKey, 0ull);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+    {
+        if (rk[j] != kEmptyKey && v[j].x == rk[j])
+            R.r[j] = make_int2((int)(uint32_t)v[j].y, (int)(uint32_t)(v[j].y >> 32));
+        else if (rk[j] != kEmptyKey && v[j].x != kEmptyKey)
+            R.r[j] = row_probe_rest(g.slots, g.hmask, rk[j], h[j]);
+    }
+    R.lo = cz - 1;
+    R.hi = cz + 1;
+    return true;
+}
+
+template <class F> __device__ __forceinline__ void grid_scan_sub(const GridDev &g, const SubRows &R, F &&f)
+{
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+    {
+        int t = R.r[j].x;
+        const int e = R.r[j].y;
+        if (t >= e)
+            continue;
+        if (e - t > 8)
+        {
+            int a = t, b = e;
+            while (a < b)
+            {
+                const int m = (a + b) >> 1;
+                if (__ldg(&g.scz[m]) < R.lo)
+                    a = m + 1;
+                else
+                    b = m;
+            }
+            t = a;
+        }
+        for (; t < e; ++t)
+        {
+            const float4 q = __ldg(&g.spos[t]);
+            const int qz = __float_as_int(q.w);
+            if (qz < R.lo)
+                continue;
+            if (qz > R.hi)
+                break;
+            f(t, q);
+        }
+    }
+}
+
+// the nearest grid point with d^2 < rr over the whole 4-lane group; every lane of
+// the group returns the same answer (ties on d^2 go to the smaller original index).
+// All 32 lanes of the warp must call it (invalid lanes pass valid = false).
+__device__ __forceinline__ NNBest nn_search_sub(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p,
+                                                float rr, bool valid)
+{
+    const int sub = threadIdx.x & (kSub - 1);
+    NNBest b{rr, -1};
+    SubRows R;
+    if (valid && grid_rows_sub(g, L, seg, o, p, sub, R))
+        grid_scan_sub(g, R, [&](int t, float4 q) {
+            const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+            if (d2 < b.d2 || (d2 == b.d2 && b.t >= 0 && __ldg(&g.sidx[t]) < __ldg(&g.sidx[b.t])))
+            {
+                b.d2 = d2;
+                b.t = t;
+            }
+        });
+#pragma unroll
+    for (int off = 1; off < kSub; off <<= 1)
+    {
+        const float od2 = __shfl_xor_sync(0xffffffffu, b.d2, off, kSub);
+        const int ot = __shfl_xor_sync(0xffffffffu, b.t, off, kSub);
+        if (ot >= 0 && (b.t < 0 || od2 < b.d2 || (od2 == b.d2 && __ldg(&g.sidx[ot]) < __ldg(&g.sidx[b.t]))))
+        {
+            b.d2 = od2;
+            b.t = ot;
+        }
+    }
     return b;
 }
 

@@ -5,11 +5,12 @@
 // (src/registration/cuda_color_icp_build_least_square.cu:134-254) and
 // solve_JTJ_JTr<true> (src/registration/eigen_solver.hpp:44-85).
 //
-// One launch per Gauss-Newton iteration covers every pair.  A block owns a chunk
-// of one pair's source points: it transforms them by the pair's current pose,
-// finds the nearest target point inside max_corr (row-hashed grid, ties to the
-// smaller index), builds the geometric and photometric residuals and their
-// 6-vector Jacobians in FP32, and accumulates the 21 + 6 + 1 system terms plus
+// Two launches per Gauss-Newton iteration cover every pair.  A block owns a chunk
+// of one pair's source points.  k_icp_nn transforms them by the pair's current pose
+// and finds the nearest target point inside max_corr (row-hashed grid, ties to the
+// smaller index); it keeps few registers so many warps hide the latency of the
+// neighbour walk.  k_icp_accum builds the geometric and photometric residuals and
+// their 6-vector Jacobians in FP32 and accumulates the 21 + 6 + 1 system terms plus
 // the correspondence count and squared distances.  Accumulation is compensated
 // FP32 inside the block (two-sum per thread and per shuffle level) and FP64 across
 // warps and blocks.  The last block of a pair to finish (atomic ticket, no
@@ -288,35 +289,43 @@ template <bool Comp> struct Acc
     }
 };
 
-// sum of the block's kTerms values into part[kTerms] (FP64 across warps when
-// compensated, FP32 otherwise); all threads must call
+// sum of the block's kTerms values into part[kTerms].  Compensated: the per-warp
+// (value, error) pairs are combined across warps by two-sum in FP32 and each of the
+// 30 results is converted to FP64 once per block (FP64 issue is ~1/64 of FP32 on
+// this part, so per-warp conversions would cost more than the sums).  Plain: FP32.
 template <bool Comp>
 __device__ __forceinline__ void block_reduce_store(Acc<Comp> &acc, double *part)
 {
-    __shared__ double s_w[kIcpThreads / 32][kTerms];
+    __shared__ float s_s[kIcpThreads / 32][kTerms];
+    __shared__ float s_e[kIcpThreads / 32][kTerms];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     acc.warp_reduce();
     if (lane == 0)
 #pragma unroll
         for (int k = 0; k < kTerms; ++k)
-            s_w[warp][k] = acc.value(k);
+        {
+            s_s[warp][k] = acc.s[k];
+            s_e[warp][k] = acc.e[k];
+        }
     __syncthreads();
     if (threadIdx.x < kTerms)
     {
-        if (Comp)
+        const int k = threadIdx.x;
+        float v = s_s[0][k], e = Comp ? s_e[0][k] : 0.0f;
+        for (int w = 1; w < kIcpThreads / 32; ++w)
         {
-            double v = 0.0;
-            for (int w = 0; w < kIcpThreads / 32; ++w)
-                v += s_w[w][threadIdx.x];
-            part[threadIdx.x] = v;
+            const float x = s_s[w][k];
+            if (Comp)
+            {
+                const float t = v + x;
+                const float bp = t - v;
+                e += s_e[w][k] + ((v - (t - bp)) + (x - bp));
+                v = t;
+            }
+            else
+                v += x;
         }
-        else
-        {
-            float v = 0.0f;
-            for (int w = 0; w < kIcpThreads / 32; ++w)
-                v += (float)s_w[w][threadIdx.x];
-            part[threadIdx.x] = (double)v;
-        }
+        part[k] = Comp ? (double)v + (double)e : (double)v;
     }
 }
 
@@ -338,11 +347,12 @@ __device__ __forceinline__ int find_pair(const int *bmap, int P, int b)
 
 // per-scale setup: block map, per-pair counts, reset of the per-scale flags
 __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-                            int chunk, int scale)
+                            int *bmap_nn, int scale)
 {
     if (threadIdx.x != 0)
         return;
-    int b = 0;
+    const int chunk = kIcpChunk;
+    int b = 0, bn = 0;
     for (int p = 0; p < P; ++p)
     {
         PairState &S = st[p];
@@ -351,6 +361,8 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
         const int nb = (ns > 0 && nt > 0) ? (ns + chunk - 1) / chunk : 0;
         bmap[p] = b;
         b += nb;
+        bmap_nn[p] = bn;
+        bn += (ns > 0 && nt > 0) ? (ns + kNNChunk - 1) / kNNChunk : 0;
         S.nblocks = nb;
         S.nsrc = ns;
         S.ntgt = nt;
@@ -374,6 +386,7 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
         }
     }
     bmap[P] = b;
+    bmap_nn[P] = bn;
 }
 
 __global__ void k_state_init(PairState *st, int P, const double *T_init)
@@ -388,57 +401,107 @@ __global__ void k_state_init(PairState *st, int P, const double *T_init)
     st[p].rmse_ref = st[p].fitness = st[p].inlier_rmse = 0.0;
 }
 
-template <bool Comp>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_iter(const float4 *__restrict__ src_pos, const int32_t *src_off,
-                                                          GridDev g, const float4 *__restrict__ attr0,
-                                                          const float4 *__restrict__ attr1, PairState *st,
-                                                          const int *bmap, int P, double *partials, IcpScale prm,
-                                                          int32_t *nn_out)
+// block -> (pair, chunk) of the pair's source points; pose as FP32 in shared memory
+struct BlockPair
 {
-    __shared__ int s_pair;
-    __shared__ float s_T[12];
-    __shared__ int s_last;
+    int pair, start, end;
+};
+
+__device__ __forceinline__ BlockPair block_pair(const int32_t *src_off, const PairState *st, const int *bmap, int P,
+                                                int chunk, float *s_T, int *s_pair)
+{
     if (threadIdx.x == 0)
     {
         int p = find_pair(bmap, P, blockIdx.x);
         if (p >= 0 && !st[p].active)
             p = -1;
-        s_pair = p;
+        *s_pair = p;
         if (p >= 0)
             for (int k = 0; k < 12; ++k)
                 s_T[k] = (float)st[p].T[k];
     }
     __syncthreads();
-    const int pair = s_pair;
-    if (pair < 0)
+    BlockPair b;
+    b.pair = *s_pair;
+    if (b.pair >= 0)
+    {
+        b.start = src_off[b.pair] + (blockIdx.x - bmap[b.pair]) * chunk;
+        b.end = min(b.start + chunk, src_off[b.pair + 1]);
+    }
+    return b;
+}
+
+__device__ __forceinline__ float3 apply_pose(const float *T, float4 s)
+{
+    return make_float3(T[0] * s.x + T[1] * s.y + T[2] * s.z + T[3], T[4] * s.x + T[5] * s.y + T[6] * s.z + T[7],
+                       T[8] * s.x + T[9] * s.y + T[10] * s.z + T[11]);
+}
+
+// step 1 of an iteration: the correspondence of every active source point
+// (grid position and squared distance, -1 when none within max_corr)
+__global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
+                                                        GridDev g, const PairState *st, const int *bmap, int P,
+                                                        float max_corr, int2 *corr, int32_t *nn_out)
+{
+    __shared__ int s_pair;
+    __shared__ float s_T[12];
+    const BlockPair b = block_pair(src_off, st, bmap, P, kNNChunk, s_T, &s_pair);
+    if (b.pair < 0)
         return;
     const KeyLayout L = *g.layout;
-    const float3 o = g.gmin[pair];
+    const float3 o = g.gmin[b.pair];
+    const float rr = __fmul_rn(max_corr, max_corr);
+    const int tbase = g.seg_off[b.pair];
+    // four lanes per source point (uniform trip count for the whole block)
+    for (int base = b.start; base < b.end; base += kIcpThreads / kSub)
+    {
+        const int i = base + (int)(threadIdx.x / kSub);
+        const bool valid = i < b.end;
+        const float3 p = apply_pose(s_T, src_pos[valid ? i : b.start]);
+        const NNBest best = nn_search_sub(g, L, b.pair, o, p, rr, valid);
+        if (valid && (threadIdx.x & (kSub - 1)) == 0)
+        {
+            corr[i] = make_int2(best.t, __float_as_int(best.d2));
+            if (nn_out)
+                nn_out[i] = best.t >= 0 ? __ldg(&g.sidx[best.t]) - tbase : -1;
+        }
+    }
+}
+
+// step 2: residuals, Jacobians, compensated block sums; the pair's last block
+// solves and updates the pose
+template <bool Comp>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restrict__ src_pos, const int32_t *src_off,
+                                                           const float4 *__restrict__ tpos,
+                                                           const float4 *__restrict__ attr0,
+                                                           const float4 *__restrict__ attr1,
+                                                           const int2 *__restrict__ corr, PairState *st,
+                                                           const int *bmap, int P, double *partials, IcpScale prm)
+{
+    __shared__ int s_pair;
+    __shared__ float s_T[12];
+    __shared__ int s_last;
+    const BlockPair b = block_pair(src_off, st, bmap, P, kIcpChunk, s_T, &s_pair);
+    const int pair = b.pair;
+    if (pair < 0)
+        return;
     const int bstart = bmap[pair];
-    const int start = src_off[pair] + (blockIdx.x - bstart) * kIcpChunk;
-    const int end = min(start + kIcpChunk, src_off[pair + 1]);
-    const int tbase = g.seg_off[pair];
-    const float rr = __fmul_rn(prm.max_corr, prm.max_corr);
     Acc<Comp> acc;
     acc.zero();
-    for (int i = start + threadIdx.x; i < end; i += kIcpThreads)
+    for (int i = b.start + threadIdx.x; i < b.end; i += kIcpThreads)
     {
-        const float4 s4 = src_pos[i];
-        const float3 p = make_float3(s_T[0] * s4.x + s_T[1] * s4.y + s_T[2] * s4.z + s_T[3],
-                                     s_T[4] * s4.x + s_T[5] * s4.y + s_T[6] * s4.z + s_T[7],
-                                     s_T[8] * s4.x + s_T[9] * s4.y + s_T[10] * s4.z + s_T[11]);
-        const NNBest best = nn_search_one(g, L, pair, o, p, rr);
-        if (nn_out)
-            nn_out[i] = best.t >= 0 ? __ldg(&g.sidx[best.t]) - tbase : -1;
-        if (best.t < 0)
+        const int2 c = corr[i];
+        if (c.x < 0)
             continue;
-        const float4 q = __ldg(&g.spos[best.t]);
-        const float4 a0 = __ldg(&attr0[best.t]);
-        const float4 a1 = __ldg(&attr1[best.t]);
+        const float4 s4 = src_pos[i];
+        const float3 p = apply_pose(s_T, s4);
+        const float4 q = __ldg(&tpos[c.x]);
+        const float4 a0 = __ldg(&attr0[c.x]);
+        const float4 a1 = __ldg(&attr1[c.x]);
         GNTerms terms;
         gn_terms(p, s4.w, make_float3(q.x, q.y, q.z), a0.w, make_float3(a0.x, a0.y, a0.z),
                  make_float3(a1.x, a1.y, a1.z), prm.sqrt_lg, prm.sqrt_lc, terms);
-        acc.add_terms(terms, best.d2);
+        acc.add_terms(terms, __int_as_float(c.y));
     }
     block_reduce_store<Comp>(acc, partials + (size_t)blockIdx.x * kTermsPad);
     __threadfence();
@@ -523,10 +586,38 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_iter(const float4 *__restri
     }
 }
 
-int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-              int scale)
+// body of the device-side iteration loop: continue while a pair is still active and
+// the scale's iteration budget lasts
+__global__ void k_icp_loop_control(const PairState *st, int P, int *iter, int max_iter,
+                                   cudaGraphConditionalHandle handle)
 {
-    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, kIcpChunk, scale);
+    __shared__ int any;
+    if (threadIdx.x == 0)
+        any = 0;
+    __syncthreads();
+    for (int p = threadIdx.x; p < P; p += blockDim.x)
+        if (st[p].active)
+            any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const int it = ++(*iter);
+        cudaGraphSetConditional(handle, (any && it < max_iter) ? 1u : 0u);
+    }
+}
+
+int icp_loop_control(gca3d_context *ctx, const PairState *st, int P, int *iter, int max_iter,
+                     cudaGraphConditionalHandle handle)
+{
+    k_icp_loop_control<<<1, 256, 0, ctx->stream>>>(st, P, iter, max_iter, handle);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
+              int *bmap_nn, int scale)
+{
+    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, bmap_nn, scale);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
@@ -539,16 +630,19 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
 }
 
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
-                  PairState *st, const int *bmap, int max_blocks, double *partials, const IcpScale &prm,
-                  bool compensated, int32_t *nn_out)
+                  PairState *st, const int *bmap, int max_blocks, const int *bmap_nn, int max_blocks_nn,
+                  double *partials, int2 *corr, const IcpScale &prm, bool compensated, int32_t *nn_out)
 {
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
+    k_icp_nn<<<max_blocks_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P,
+                                                             prm.max_corr, corr, nn_out);
+    GCA_CHECK_LAUNCH(ctx);
     if (compensated)
-        k_icp_iter<true><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, attr0, attr1, st,
-                                                                      bmap, src.P, partials, prm, nn_out);
+        k_icp_accum<true><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
+                                                                       corr, st, bmap, src.P, partials, prm);
     else
-        k_icp_iter<false><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, attr0, attr1, st,
-                                                                       bmap, src.P, partials, prm, nn_out);
+        k_icp_accum<false><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0,
+                                                                        attr1, corr, st, bmap, src.P, partials, prm);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidIcpIter);
     return GCA3D_OK;

@@ -7,7 +7,8 @@ namespace gca3d
 {
 
 constexpr int kIcpThreads = 256;
-constexpr int kIcpChunk = 1024; // source points per block
+constexpr int kIcpChunk = 1024; // source points per accumulate block (one partial each)
+constexpr int kNNChunk = 256;   // source points per NN block (many short blocks hide latency)
 constexpr int kTerms = 30;      // 21 JTJ (upper) + 6 JTr + r^2 + correspondences + sum d^2
 constexpr int kTermsPad = 32;
 
@@ -46,10 +47,12 @@ __global__ void __launch_bounds__(kIcpThreads)
 
 int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit);
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-              int scale);
+              int *bmap_nn, int scale);
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
-                  PairState *st, const int *bmap, int max_blocks, double *partials, const IcpScale &prm,
-                  bool compensated, int32_t *nn_out);
+                  PairState *st, const int *bmap, int max_blocks, const int *bmap_nn, int max_blocks_nn,
+                  double *partials, int2 *corr, const IcpScale &prm, bool compensated, int32_t *nn_out);
+int icp_loop_control(gca3d_context *ctx, const PairState *st, int P, int *iter, int max_iter,
+                     cudaGraphConditionalHandle handle);
 int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
              double *out30);
 int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,

@@ -206,6 +206,35 @@ __device__ __forceinline__ int cell_of(float p, float mn, float cell)
 
 __device__ __forceinline__ int bitlen_u32(uint32_t v) { return v ? 32 - __clz(v) : 0; }
 
+// block-wide min/max of 3 components, then one atomic per component per block
+// (per-warp atomics on the same few words serialise in one L2 slice)
+__device__ __forceinline__ void block_bounds_commit(float mn[3], float mx[3], int *ord6)
+{
+    __shared__ float s_mn[3][32], s_mx[3][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
+            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
+        }
+    if (lane == 0)
+        for (int a = 0; a < 3; ++a)
+            s_mn[a][warp] = mn[a], s_mx[a][warp] = mx[a];
+    __syncthreads();
+    if (threadIdx.x < 3)
+    {
+        const int a = threadIdx.x;
+        float m = s_mn[a][0], M = s_mx[a][0];
+        for (int w = 1; w < nw; ++w)
+            m = fminf(m, s_mn[a][w]), M = fmaxf(M, s_mx[a][w]);
+        atomicMin(ord6 + a, float_to_ordered(m));
+        atomicMax(ord6 + 3 + a, float_to_ordered(M));
+    }
+}
+
 template <typename T> __device__ __forceinline__ T warp_sum(T v)
 {
 #pragma unroll
@@ -237,6 +266,15 @@ struct KeyLayout
     int total_bits;
 };
 
+// one open-addressing slot of the row hash: the key and the row's [start, end) in
+// the sorted arrays, read with a single 16-byte load
+struct __align__(16) RowSlot
+{
+    unsigned long long key;
+    int start;
+    int end;
+};
+
 // a grid over the target segments
 struct GridDev
 {
@@ -248,10 +286,10 @@ struct GridDev
     float4 *spos;  // x, y, z, __int_as_float(cz)
     int32_t *sidx; // batch index of the point (original order)
     float *sint;   // intensity in sorted order
+    int *scz;      // z cell in sorted order (compact copy for the in-row binary search)
     uint64_t *skey;
-    // row hash: key = (seg, cx, cy) -> [start, end)
-    unsigned long long *hkeys;
-    int2 *hvals;
+    // row hash: key = (seg, cx, cy) -> [start, end) in one 16-byte slot
+    RowSlot *slots;
     uint32_t hmask;
     const int32_t *seg_off; // [P + 1] offsets of the segments in the sorted arrays
 };
@@ -268,18 +306,22 @@ __device__ __forceinline__ uint32_t hash_u64(unsigned long long k)
     return (uint32_t)k;
 }
 
-__device__ __forceinline__ int2 row_lookup(const unsigned long long *hkeys, const int2 *hvals,
-                                           uint32_t hmask, unsigned long long rk)
+__device__ __forceinline__ ulonglong2 slot_load(const RowSlot *slots, uint32_t h)
 {
-    uint32_t h = hash_u64(rk) & hmask;
-    for (uint32_t probe = 0; probe <= hmask; ++probe)
+    return __ldg(reinterpret_cast<const ulonglong2 *>(slots + h));
+}
+
+// continue a linear probe after the first slot missed
+static __device__ __noinline__ int2 row_probe_rest(const RowSlot *slots, uint32_t hmask, unsigned long long rk, uint32_t h)
+{
+    for (uint32_t probe = 1; probe <= hmask; ++probe)
     {
-        unsigned long long k = __ldg(hkeys + h);
-        if (k == rk)
-            return __ldg(hvals + h);
-        if (k == kEmptyKey)
-            break;
         h = (h + 1) & hmask;
+        const ulonglong2 v = slot_load(slots, h);
+        if (v.x == rk)
+            return make_int2((int)(uint32_t)v.y, (int)(uint32_t)(v.y >> 32));
+        if (v.x == kEmptyKey)
+            break;
     }
     return make_int2(0, 0);
 }

@@ -9,8 +9,11 @@
 // registers; no lists exist.  Moments are taken about the query point, so the
 // FP32 covariance does not cancel at metre-scale coordinates (the reference's
 // E[xx^T] - E[x]E[x]^T does).  The 3x3 eigen-problem is solved in closed form in
-// FP32; when the two smallest eigenvalues are close the covariance is rebuilt in
-// FP64 and solved by Jacobi rotations.  The gradient follows the reference's
+// FP32; points whose two smallest eigenvalues are close (about 0.2 % of surface
+// points) are queued and redone by a second kernel with the covariance rebuilt in
+// FP64 and Jacobi rotations -- densely, one point per thread, because FP64 issues
+// at a small fraction of the FP32 rate here and a divergent fallback inside the
+// FP32 kernel would stall whole warps.  A third kernel computes the gradients.  The gradient follows the reference's
 // system: tangent-plane least squares, (knn - 1)^2 n n^T orthogonality term,
 // 1e-6 ridge, LDL^T solve (in the tangent/normal basis, see solve_gradient_system).
 #include "grid_query.cuh"
@@ -95,7 +98,7 @@ __device__ bool smallest_eigvec_f32(float a00, float a01, float a02, float a11, 
     const float lmax = q + 2.0f * p * cosf(phi);
     const float lmin = q + 2.0f * p * cosf(phi + 2.0943951023931957f);
     const float lmid = 3.0f * q - lmax - lmin;
-    if (!(lmid - lmin > 1e-2f * (lmax - lmin)))
+    if (!(lmid - lmin > 1e-3f * (lmax - lmin)))
         return false;
     const float3 r0 = make_float3(a00 - lmin, a01, a02);
     const float3 r1 = make_float3(a01, a11 - lmin, a12);
@@ -181,16 +184,172 @@ struct NbrEntry
     int t;   // grid position
 };
 
-__global__ void __launch_bounds__(256) k_normals_grad(GridDev g, const int32_t *d_n, int do_normals, float rn,
-                                                      int max_nn, int do_grad, float rg, const float4 *in_nrm,
-                                                      float4 *attr0, float4 *attr1, float4 *nrm_out,
-                                                      float4 *grd_out)
+// the max_nn nearest neighbours inside rn2 (distance, then index), ascending
+__device__ __forceinline__ int select_knn(const GridDev &g, const GridRows &R, float3 p, float rn2, int max_nn,
+                                          NbrEntry *list)
+{
+    int cnt = 0;
+    grid_scan(g, R, [&](int t, float4 q) {
+        const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+        if (!(d2 < rn2))
+            return;
+        const int idx = g.sidx[t];
+        if (cnt == max_nn)
+        {
+            const NbrEntry &w = list[cnt - 1];
+            if (!(d2 < w.d2 || (d2 == w.d2 && idx < w.idx)))
+                return;
+            --cnt;
+        }
+        int j = cnt;
+        while (j > 0 && (list[j - 1].d2 > d2 || (list[j - 1].d2 == d2 && list[j - 1].idx > idx)))
+        {
+            list[j] = list[j - 1];
+            --j;
+        }
+        list[j] = NbrEntry{d2, idx, t};
+        ++cnt;
+    });
+    return cnt;
+}
+
+struct NormalOut
+{
+    float4 *attr0;    // grid order {n, intensity}, or null
+    float4 *nrm_out;  // original order {n, 0}, or null
+    int *degen_count; // near-degenerate points, appended for the FP64 pass
+    int *degen_list;
+};
+
+__device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, float3 n, float Ip)
+{
+    if (O.attr0)
+        O.attr0[s] = make_float4(n.x, n.y, n.z, Ip);
+    if (O.nrm_out)
+        O.nrm_out[gi] = make_float4(n.x, n.y, n.z, 0.0f);
+}
+
+// pass 1: PCA normal per grid point in FP32 -- moments about the query point,
+// closed-form eigen-system; points whose smallest eigenvalue is not separated by
+// 1e-3 of the spread are queued for the FP64 pass
+__global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n, float rn, int max_nn, NormalOut O)
 {
     const int n = *d_n;
     const KeyLayout L = *g.layout;
     const int segshift = L.bx + L.by + L.bz;
-    const float rn2 = __fmul_rn(rn, rn), rg2 = __fmul_rn(rg, rg);
+    const float rn2 = __fmul_rn(rn, rn);
     NbrEntry list[kMaxNN];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        const float4 p4 = g.spos[s];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
+        const int seg = L.bseg ? (int)(g.skey[s] >> segshift) : 0;
+        GridRows R;
+        const bool inside = grid_rows(g, L, seg, g.gmin[seg], p, R);
+        float s1x = 0, s1y = 0, s1z = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
+        int k = 0;
+        auto acc = [&](float4 q) {
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            s1x += dx, s1y += dy, s1z += dz;
+            sxx += dx * dx, sxy += dx * dy, sxz += dx * dz;
+            syy += dy * dy, syz += dy * dz, szz += dz * dz;
+            ++k;
+        };
+        if (inside && max_nn <= 0)
+            grid_scan(g, R, [&](int t, float4 q) {
+                if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                    acc(q);
+            });
+        else if (inside)
+        {
+            const int cnt = select_knn(g, R, p, rn2, max_nn, list);
+            for (int j = 0; j < cnt; ++j)
+                acc(g.spos[list[j].t]);
+        }
+        float3 nrm = make_float3(0.0f, 0.0f, 0.0f);
+        if (k >= 3)
+        {
+            const float ik = 1.0f / (float)k;
+            const float mx = s1x * ik, my = s1y * ik, mz = s1z * ik;
+            if (!smallest_eigvec_f32(sxx * ik - mx * mx, sxy * ik - mx * my, sxz * ik - mx * mz, syy * ik - my * my,
+                                     syz * ik - my * mz, szz * ik - mz * mz, nrm))
+            {
+                O.degen_list[atomicAdd(O.degen_count, 1)] = s;
+                continue; // written by the FP64 pass
+            }
+            // orient against (0, 0, -1) (cuda_estimate_normals.cu:131-151)
+            if (nrm.z > 0.0f)
+                nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+        }
+        store_normal(O, s, g.sidx[s], nrm, g.sint[s]);
+    }
+}
+
+// pass 2: the queued near-degenerate points, one per thread (no divergence with
+// the FP32 majority): covariance rebuilt in FP64 from the same neighbours, Jacobi
+__global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_nn, NormalOut O)
+{
+    const int n = *O.degen_count;
+    const KeyLayout L = *g.layout;
+    const int segshift = L.bx + L.by + L.bz;
+    const float rn2 = __fmul_rn(rn, rn);
+    NbrEntry list[kMaxNN];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    {
+        const int s = O.degen_list[j];
+        const float4 p4 = g.spos[s];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
+        const int seg = L.bseg ? (int)(g.skey[s] >> segshift) : 0;
+        GridRows R;
+        grid_rows(g, L, seg, g.gmin[seg], p, R);
+        double S1[3] = {0, 0, 0}, S2[6] = {0, 0, 0, 0, 0, 0};
+        int k = 0;
+        auto acc = [&](float4 q) {
+            const double dx = (double)q.x - (double)p.x, dy = (double)q.y - (double)p.y, dz = (double)q.z - (double)p.z;
+            S1[0] += dx, S1[1] += dy, S1[2] += dz;
+            S2[0] += dx * dx, S2[1] += dx * dy, S2[2] += dx * dz;
+            S2[3] += dy * dy, S2[4] += dy * dz, S2[5] += dz * dz;
+            ++k;
+        };
+        if (max_nn <= 0)
+            grid_scan(g, R, [&](int t, float4 q) {
+                if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                    acc(q);
+            });
+        else
+        {
+            const int cnt = select_knn(g, R, p, rn2, max_nn, list);
+            for (int i = 0; i < cnt; ++i)
+                acc(g.spos[list[i].t]);
+        }
+        const double kk = (double)k;
+        const double mu[3] = {S1[0] / kk, S1[1] / kk, S1[2] / kk};
+        double C[3][3];
+        C[0][0] = S2[0] / kk - mu[0] * mu[0];
+        C[0][1] = C[1][0] = S2[1] / kk - mu[0] * mu[1];
+        C[0][2] = C[2][0] = S2[2] / kk - mu[0] * mu[2];
+        C[1][1] = S2[3] / kk - mu[1] * mu[1];
+        C[1][2] = C[2][1] = S2[4] / kk - mu[1] * mu[2];
+        C[2][2] = S2[5] / kk - mu[2] * mu[2];
+        double v[3];
+        jacobi_smallest(C, v);
+        float3 nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
+        if (nrm.z > 0.0f)
+            nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+        store_normal(O, s, g.sidx[s], nrm, g.sint[s]);
+    }
+}
+
+// pass 3: colour gradient per grid point (the reference's system, solved in the
+// tangent/normal basis); the normal comes from grid-order attr0 or from an
+// original-order array
+__global__ void __launch_bounds__(256) k_gradient(GridDev g, const int32_t *d_n, float rg, const float4 *nrm_grid,
+                                                  const float4 *nrm_orig, float4 *attr1, float4 *grd_out)
+{
+    const int n = *d_n;
+    const KeyLayout L = *g.layout;
+    const int segshift = L.bx + L.by + L.bz;
+    const float rg2 = __fmul_rn(rg, rg);
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
         const float4 p4 = g.spos[s];
@@ -198,140 +357,66 @@ __global__ void __launch_bounds__(256) k_normals_grad(GridDev g, const int32_t *
         const int gi = g.sidx[s];
         const float Ip = g.sint[s];
         const int seg = L.bseg ? (int)(g.skey[s] >> segshift) : 0;
-        const float3 o = g.gmin[seg];
-        float3 nrm = make_float3(0.0f, 0.0f, 0.0f);
-        if (do_normals)
-        {
-            float s1x = 0, s1y = 0, s1z = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
-            int k = 0;
-            if (max_nn <= 0)
-            {
-                grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
-                    if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
-                    {
-                        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-                        s1x += dx, s1y += dy, s1z += dz;
-                        sxx += dx * dx, sxy += dx * dy, sxz += dx * dz;
-                        syy += dy * dy, syz += dy * dz, szz += dz * dz;
-                        ++k;
-                    }
-                });
-            }
-            else
-            {
-                int cnt = 0;
-                grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
-                    const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
-                    if (!(d2 < rn2))
-                        return;
-                    const int idx = g.sidx[t];
-                    if (cnt == max_nn)
-                    {
-                        const NbrEntry &w = list[cnt - 1];
-                        if (!(d2 < w.d2 || (d2 == w.d2 && idx < w.idx)))
-                            return;
-                        --cnt;
-                    }
-                    int j = cnt;
-                    while (j > 0 && (list[j - 1].d2 > d2 || (list[j - 1].d2 == d2 && list[j - 1].idx > idx)))
-                    {
-                        list[j] = list[j - 1];
-                        --j;
-                    }
-                    list[j] = NbrEntry{d2, idx, t};
-                    ++cnt;
-                });
-                for (int j = 0; j < cnt; ++j)
-                {
-                    const float4 q = g.spos[list[j].t];
-                    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-                    s1x += dx, s1y += dy, s1z += dz;
-                    sxx += dx * dx, sxy += dx * dy, sxz += dx * dz;
-                    syy += dy * dy, syz += dy * dz, szz += dz * dz;
-                }
-                k = cnt;
-            }
-            if (k >= 3)
-            {
-                const float ik = 1.0f / (float)k;
-                const float mx = s1x * ik, my = s1y * ik, mz = s1z * ik;
-                const float c00 = sxx * ik - mx * mx, c01 = sxy * ik - mx * my, c02 = sxz * ik - mx * mz;
-                const float c11 = syy * ik - my * my, c12 = syz * ik - my * mz, c22 = szz * ik - mz * mz;
-                if (!smallest_eigvec_f32(c00, c01, c02, c11, c12, c22, nrm))
-                {
-                    // near-degenerate: rebuild the covariance in FP64 and use Jacobi
-                    double S1[3] = {0, 0, 0}, S2[3][3] = {{0}};
-                    int kk = 0;
-                    auto acc = [&](float4 q) {
-                        const double d[3] = {(double)q.x - (double)p.x, (double)q.y - (double)p.y,
-                                             (double)q.z - (double)p.z};
-                        for (int a = 0; a < 3; ++a)
-                        {
-                            S1[a] += d[a];
-                            for (int b = 0; b < 3; ++b)
-                                S2[a][b] += d[a] * d[b];
-                        }
-                        ++kk;
-                    };
-                    if (max_nn <= 0)
-                        grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
-                            if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
-                                acc(q);
-                        });
-                    else
-                        for (int j = 0; j < k; ++j)
-                            acc(g.spos[list[j].t]);
-                    double C[3][3], mu[3];
-                    for (int a = 0; a < 3; ++a)
-                        mu[a] = S1[a] / kk;
-                    for (int a = 0; a < 3; ++a)
-                        for (int b = 0; b < 3; ++b)
-                            C[a][b] = S2[a][b] / kk - mu[a] * mu[b];
-                    double v[3];
-                    jacobi_smallest(C, v);
-                    nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
-                }
-                // orient against (0, 0, -1) (cuda_estimate_normals.cu:131-151)
-                if (nrm.z > 0.0f)
-                    nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
-            }
-            if (nrm_out)
-                nrm_out[gi] = make_float4(nrm.x, nrm.y, nrm.z, 0.0f);
-        }
-        else
-        {
-            const float4 q = in_nrm[gi];
-            nrm = make_float3(q.x, q.y, q.z);
-        }
+        const float4 n4 = nrm_grid ? nrm_grid[s] : nrm_orig[gi];
+        const float3 nrm = make_float3(n4.x, n4.y, n4.z);
+        int knn = 0;
+        float A00 = 0, A01 = 0, A02 = 0, A11 = 0, A12 = 0, A22 = 0, b0 = 0, b1 = 0, b2 = 0;
+        grid_visit(g, L, seg, g.gmin[seg], p, [&](int t, float4 q) {
+            if (!(dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rg2))
+                return;
+            ++knn;
+            if (t == s)
+                return;
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            const float sp = dx * nrm.x + dy * nrm.y + dz * nrm.z;
+            const float vx = dx - sp * nrm.x, vy = dy - sp * nrm.y, vz = dz - sp * nrm.z;
+            const float dI = g.sint[t] - Ip;
+            A00 += vx * vx, A01 += vx * vy, A02 += vx * vz;
+            A11 += vy * vy, A12 += vy * vz, A22 += vz * vz;
+            b0 += vx * dI, b1 += vy * dI, b2 += vz * dI;
+        });
         float3 grad = make_float3(0.0f, 0.0f, 0.0f);
-        if (do_grad)
-        {
-            int knn = 0;
-            float A00 = 0, A01 = 0, A02 = 0, A11 = 0, A12 = 0, A22 = 0, b0 = 0, b1 = 0, b2 = 0;
-            grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
-                if (!(dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rg2))
-                    return;
-                ++knn;
-                if (t == s)
-                    return;
-                const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-                const float sp = dx * nrm.x + dy * nrm.y + dz * nrm.z;
-                const float vx = dx - sp * nrm.x, vy = dy - sp * nrm.y, vz = dz - sp * nrm.z;
-                const float dI = g.sint[t] - Ip;
-                A00 += vx * vx, A01 += vx * vy, A02 += vx * vz;
-                A11 += vy * vy, A12 += vy * vz, A22 += vz * vz;
-                b0 += vx * dI, b1 += vy * dI, b2 += vz * dI;
-            });
-            if (knn >= 5)
-                grad = solve_gradient_system(A00, A01, A02, A11, A12, A22, b0, b1, b2, nrm,
-                                             (float)((knn - 1) * (knn - 1)));
-            if (grd_out)
-                grd_out[gi] = make_float4(grad.x, grad.y, grad.z, 0.0f);
-        }
-        if (attr0)
-            attr0[s] = make_float4(nrm.x, nrm.y, nrm.z, Ip);
+        if (knn >= 5)
+            grad = solve_gradient_system(A00, A01, A02, A11, A12, A22, b0, b1, b2, nrm,
+                                         (float)((knn - 1) * (knn - 1)));
         if (attr1)
             attr1[s] = make_float4(grad.x, grad.y, grad.z, 0.0f);
+        if (grd_out)
+            grd_out[gi] = make_float4(grad.x, grad.y, grad.z, 0.0f);
+    }
+}
+
+// ICP target records in another grid's order: {normal, intensity}, {gradient, 0}
+__global__ void k_gather_attrs(GridDev g, const int32_t *d_n, const float4 *__restrict__ nrm,
+                               const float4 *__restrict__ grd, float4 *attr0, float4 *attr1)
+{
+    const int n = *d_n;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        const int gi = g.sidx[s];
+        const float4 a = nrm[gi], d = grd[gi];
+        attr0[s] = make_float4(a.x, a.y, a.z, g.sint[s]);
+        attr1[s] = make_float4(d.x, d.y, d.z, 0.0f);
+    }
+}
+
+int gather_attrs(gca3d_context *ctx, const Batch &b, const Grid &g, const float4 *nrm, const float4 *grd,
+                 float4 *attr0, float4 *attr1)
+{
+    const int gs = std::min(grid_for(g.cap), ctx->num_sms * 8);
+    k_gather_attrs<<<gs, kBlock, 0, ctx->stream>>>(g.dev, b.seg_off + b.P, nrm, grd, attr0, attr1);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+// grid-order {normal, intensity} records from original-order normals
+__global__ void k_attr0_from(GridDev g, const int32_t *d_n, const float4 *__restrict__ nrm, float4 *attr0)
+{
+    const int n = *d_n;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+    {
+        const float4 a = nrm[g.sidx[s]];
+        attr0[s] = make_float4(a.x, a.y, a.z, g.sint[s]);
     }
 }
 
@@ -347,11 +432,40 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gradient: radius must be in (0, grid cell]");
     if (!do_normals && !in_nrm)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gradient: normals needed");
+    if (do_grad && do_normals && !attr0 && !nrm_out)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "gradient: the normals must be stored");
+    const int32_t *d_n = b.seg_off + b.P;
     const int gs = std::min(grid_for(g.cap), ctx->num_sms * 8);
     GCA_PROF_BEGIN(ctx, kKidNormals);
-    k_normals_grad<<<gs, 256, 0, ctx->stream>>>(g.dev, b.seg_off + b.P, do_normals ? 1 : 0, normal_radius, max_nn,
-                                                do_grad ? 1 : 0, grad_radius, in_nrm, attr0, attr1, nrm_out, grd_out);
-    GCA_CHECK_LAUNCH(ctx);
+    if (do_normals)
+    {
+        NormalOut O;
+        O.attr0 = attr0;
+        O.nrm_out = nrm_out;
+        O.degen_count = ctx->arena.get<int>(1);
+        O.degen_list = ctx->arena.get<int>(std::max<int64_t>(g.cap, 1));
+        if (!O.degen_count || !O.degen_list)
+            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "normals: scratch");
+        GCA_CUDA(ctx, cudaMemsetAsync(O.degen_count, 0, sizeof(int), ctx->stream));
+        k_normals32<<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
+        GCA_CHECK_LAUNCH(ctx);
+        k_normals64<<<ctx->num_sms, 128, 0, ctx->stream>>>(g.dev, normal_radius, max_nn, O);
+        GCA_CHECK_LAUNCH(ctx);
+    }
+    if (do_grad)
+    {
+        const float4 *ng = do_normals ? attr0 : nullptr;
+        const float4 *no = do_normals ? (attr0 ? nullptr : nrm_out) : in_nrm;
+        k_gradient<<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, grad_radius, ng, no, attr1, grd_out);
+        GCA_CHECK_LAUNCH(ctx);
+    }
+    else if (attr1)
+        GCA_CUDA(ctx, cudaMemsetAsync(attr1, 0, sizeof(float4) * g.cap, ctx->stream));
+    if (!do_normals && attr0)
+    {
+        k_attr0_from<<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, in_nrm, attr0);
+        GCA_CHECK_LAUNCH(ctx);
+    }
     GCA_PROF_END(ctx, kKidNormals);
     return GCA3D_OK;
 }

@@ -5,13 +5,15 @@
 // (apps/test_color_icp.cpp:378-400).
 //
 // Per scale, for all pairs at once: voxel-downsample sources and targets (or copy
-// them when the scale has no voxel size), build one target grid (cell = the
-// largest radius used), estimate target normals and colour gradients in grid
-// order, then launch one fused ICP kernel per iteration.  Nothing on the way
+// them when the scale has no voxel size), build the target grid for normals and
+// colour gradients (cell = their largest radius) and, when the correspondence
+// distance is smaller, a second, tighter target grid for the NN search; estimate
+// target normals and gradients, then launch the two ICP kernels per iteration.  Nothing on the way
 // synchronises with the host unless the plain mode is chosen, which, like the
 // reference, checks convergence on the host after every iteration.  A plan runs
 // the schedule once to size its scratch memory and then captures it as one CUDA
-// graph that execute replays.
+// graph that execute replays; in the graph each scale's iteration loop is a
+// conditional WHILE node, so the device stops iterating once every pair converged.
 #include "icp.cuh"
 #include "stages.cuh"
 
@@ -39,11 +41,14 @@ struct gca3d_icp_plan
     PairState *h_state = nullptr;
     double *d_Tinit = nullptr, *h_Tinit = nullptr;
     int max_blocks = 0;
+    int max_blocks_nn = 0;
     int64_t src_cap = 0, tgt_cap = 0, src_max = 0, tgt_max = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int64_t kernels_per_run = 0;
+    int64_t kernels_static = 0; // graph kernels outside the iteration loops
     bool host_checks = false; // plain mode: convergence test read back after every iteration
+    cudaStream_t side = nullptr; // captures the bodies of the device-side loops
 };
 
 namespace
@@ -111,22 +116,40 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             if ((st = gather_stage(ctx, pl->d_tgt, P, pl->tgt_max, bt, keep)))
                 return st;
         }
-        float cell = std::max(S.max_corr, S.grad_radius);
+        // the normals / gradient grid (cell = largest of their radii) and, when the
+        // correspondence distance is smaller, a tighter grid for the NN search
+        float cell_n = S.grad_radius;
         if (!keep)
-            cell = std::max(cell, S.normal_radius);
-        Grid g;
-        if ((st = grid_build(ctx, bt, cell, kOriginPadF32, nullptr, g)))
+            cell_n = std::max(cell_n, S.normal_radius);
+        const bool own_nn_grid = S.max_corr < 0.9f * cell_n;
+        Grid g, gnn;
+        if ((st = grid_build(ctx, bt, std::max(cell_n, own_nn_grid ? 0.0f : S.max_corr), kOriginPadF32, nullptr, g)))
             return st;
+        if (own_nn_grid && (st = grid_build(ctx, bt, S.max_corr, kOriginPadF32, nullptr, gnn)))
+            return st;
+        const Grid &gicp = own_nn_grid ? gnn : g;
         float4 *attr0 = ctx->arena.get<float4>(g.cap);
         float4 *attr1 = ctx->arena.get<float4>(g.cap);
         double *partials = ctx->arena.get<double>((size_t)std::max(pl->max_blocks, 1) * kTermsPad);
+        int2 *corr = ctx->arena.get<int2>(std::max<int64_t>(bs.cap, 1));
         int *bmap = ctx->arena.get<int>(P + 1);
-        if (!attr0 || !attr1 || !partials || !bmap)
+        int *bmap_nn = ctx->arena.get<int>(P + 1);
+        float4 *nrm_b = own_nn_grid && !keep ? ctx->arena.get<float4>(g.cap) : nullptr;
+        float4 *grd_b = own_nn_grid ? ctx->arena.get<float4>(g.cap) : nullptr;
+        if (!attr0 || !attr1 || !partials || !corr || !bmap || !bmap_nn || (own_nn_grid && (!grd_b || (!keep && !nrm_b))))
             return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
-        if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
-                                keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
+        if (own_nn_grid)
+        {
+            if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
+                                    keep ? bt.nrm : nullptr, nullptr, nullptr, nrm_b, grd_b)))
+                return st;
+            if ((st = gather_attrs(ctx, bt, gnn, keep ? bt.nrm : nrm_b, grd_b, attr0, attr1)))
+                return st;
+        }
+        else if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
+                                     keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
             return st;
-        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, si)))
+        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, bmap_nn, si)))
             return st;
         IcpScale prm;
         prm.max_corr = S.max_corr;
@@ -135,10 +158,53 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         prm.update_map = p.update_map;
         prm.rot_eps = p.rot_eps;
         prm.trans_eps = p.trans_eps;
+        int *iter = ctx->arena.get<int>(1); // loop counter of the captured loop (same arena layout eager)
+        if (!iter)
+            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
+        if (capturing && S.max_iter > 0)
+        {
+            // the iteration loop as a device-side WHILE node: the body runs while a
+            // pair is active and the budget lasts, so converged schedules stop early
+            GCA_CUDA(ctx, cudaMemsetAsync(iter, 0, sizeof(int), ctx->stream));
+            cudaStreamCaptureStatus cs;
+            cudaGraph_t cg = nullptr;
+            const cudaGraphNode_t *deps = nullptr;
+            size_t nd = 0;
+            GCA_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, nullptr, &nd));
+            cudaGraphConditionalHandle handle;
+            GCA_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams np = {};
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = handle;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t node;
+            GCA_CUDA(ctx, cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np));
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            cudaStream_t main_stream = ctx->stream;
+            GCA_CUDA(ctx, cudaStreamBeginCaptureToGraph(pl->side, body, nullptr, nullptr, 0,
+                                                        cudaStreamCaptureModeThreadLocal));
+            ctx->stream = pl->side;
+            const int64_t l0 = ctx->launches;
+            st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
+                               pl->max_blocks_nn, partials, corr, prm, p.compensated != 0, nullptr);
+            if (!st)
+                st = icp_loop_control(ctx, pl->d_state, P, iter, S.max_iter, handle);
+            pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
+            ctx->stream = main_stream;
+            cudaGraph_t captured = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(pl->side, &captured);
+            if (st)
+                return st;
+            GCA_CUDA(ctx, e);
+            GCA_CUDA(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1,
+                                                              cudaStreamSetCaptureDependencies));
+            continue;
+        }
         for (int it = 0; it < S.max_iter; ++it)
         {
-            if ((st = icp_iteration(ctx, bs, g, attr0, attr1, pl->d_state, bmap, pl->max_blocks, partials, prm,
-                                    p.compensated != 0, nullptr)))
+            if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
+                                    pl->max_blocks_nn, partials, corr, prm, p.compensated != 0, nullptr)))
                 return st;
             if (pl->host_checks && !capturing)
             {
@@ -161,10 +227,13 @@ int run_with_arena(gca3d_icp_plan *pl, bool capturing)
     pl->ctx->arena.swap(pl->arena);
     pl->ctx->arena.reset();
     const int64_t l0 = pl->ctx->launches;
+    pl->kernels_static = 0;
     int st = run_schedule(pl, capturing);
     if (!st && pl->ctx->arena.failed)
         st = fail(pl->ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp plan: scratch memory");
     pl->kernels_per_run = pl->ctx->launches - l0;
+    if (capturing)
+        pl->kernels_static += pl->kernels_per_run;
     pl->ctx->arena.swap(pl->arena);
     return st;
 }
@@ -205,6 +274,8 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
         cudaStreamSynchronize(pl->ctx->stream);
     if (pl->exec)
         cudaGraphExecDestroy(pl->exec);
+    if (pl->side)
+        cudaStreamDestroy(pl->side);
     if (pl->graph)
         cudaGraphDestroy(pl->graph);
     cudaFree(pl->d_src);
@@ -251,8 +322,10 @@ static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d
         pl->src_max = std::max(pl->src_max, src[k]->capacity);
         pl->tgt_max = std::max(pl->tgt_max, tgt[k]->capacity);
         nb += div_up(src[k]->capacity, kIcpChunk);
+        pl->max_blocks_nn += div_up(src[k]->capacity, kNNChunk);
     }
     pl->max_blocks = std::max(nb, 1);
+    pl->max_blocks_nn = std::max(pl->max_blocks_nn, 1);
     // device tables and state live outside the scratch arena
     std::vector<SegSrc> hs(P), ht(P);
     for (int k = 0; k < P; ++k)
@@ -277,6 +350,12 @@ static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d
         for (int j = 0; j < 16; ++j)
             pl->h_Tinit[16 * k + j] = (j % 5 == 0) ? 1.0 : 0.0;
     cudaMemcpy(pl->d_Tinit, pl->h_Tinit, sizeof(double) * 16 * P, cudaMemcpyHostToDevice);
+    if (capture && cudaStreamCreateWithFlags(&pl->side, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        cudaGetLastError();
+        gca3d_icp_plan_destroy(pl);
+        return fail(ctx, GCA3D_ERR_CUDA, "icp plan: side stream");
+    }
     if (capture)
     {
         // size the scratch with one eager run, then capture the identical sequence
@@ -307,6 +386,11 @@ static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d
                     e = cudaGraphInstantiate(&pl->exec, pl->graph, 0);
                     if (e != cudaSuccess)
                         st = cuda_fail(ctx, e, "cudaGraphInstantiate");
+                    // until an execute reports iteration counts: every loop runs to its budget
+                    int64_t budget = 0;
+                    for (int s = 0; s < params->n_scales; ++s)
+                        budget += params->scales[s].max_iter;
+                    pl->kernels_per_run = pl->kernels_static + 3 * budget;
                 }
             }
             pl->arena.frozen = false;
@@ -342,7 +426,8 @@ int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_r
     if (pl->exec)
     {
         GCA_CUDA(ctx, cudaGraphLaunch(pl->exec, ctx->stream));
-        ctx->launches += pl->kernels_per_run;
+        if (!results) // iteration counts unknown: the previous execute's count stands in
+            ctx->launches += pl->kernels_per_run;
     }
     else if ((st = run_with_arena(pl, false)))
         return st;
@@ -353,6 +438,19 @@ int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_r
     if ((st = consume_device_error(ctx, "icp")))
         return st;
     fill_results(pl, results);
+    if (pl->exec)
+    {
+        int64_t loops = 0;
+        for (int s = 0; s < pl->prm.n_scales; ++s)
+        {
+            int m = 0;
+            for (int k = 0; k < pl->P; ++k)
+                m = std::max(m, pl->h_state[k].scale_iters[s]);
+            loops += pl->prm.scales[s].max_iter > 0 ? std::max(m, 1) : 0;
+        }
+        pl->kernels_per_run = pl->kernels_static + 3 * loops;
+        ctx->launches += pl->kernels_per_run;
+    }
     return GCA3D_OK;
 }
 

@@ -71,6 +71,10 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
                   int max_nn, bool do_grad, float grad_radius, const float4 *in_nrm, float4 *attr0,
                   float4 *attr1, float4 *nrm_out, float4 *grd_out);
 
+// the target records of grid g gathered from original-order normals / gradients
+int gather_attrs(gca3d_context *ctx, const Batch &b, const Grid &g, const float4 *nrm, const float4 *grd,
+                 float4 *attr0, float4 *attr1);
+
 // nearest neighbour / radius lists of query batch points against a single-segment grid
 int nn_query(gca3d_context *ctx, const float4 *qpos, const int32_t *d_nq, int64_t qcap, const Grid &g,
              float radius, int32_t *out_idx);

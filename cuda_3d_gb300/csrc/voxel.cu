@@ -79,6 +79,8 @@ __global__ void k_src_bounds(const SegSrc *src, int *ord)
 {
     const int seg = blockIdx.y;
     const int n = *src[seg].d_n;
+    if ((int64_t)blockIdx.x * blockDim.x >= n)
+        return;
     const float4 *pos = src[seg].pos;
     float mn[3] = {3.402823466e38f, 3.402823466e38f, 3.402823466e38f};
     float mx[3] = {-3.402823466e38f, -3.402823466e38f, -3.402823466e38f};
@@ -88,20 +90,7 @@ __global__ void k_src_bounds(const SegSrc *src, int *ord)
         mn[0] = fminf(mn[0], p.x), mn[1] = fminf(mn[1], p.y), mn[2] = fminf(mn[2], p.z);
         mx[0] = fmaxf(mx[0], p.x), mx[1] = fmaxf(mx[1], p.y), mx[2] = fmaxf(mx[2], p.z);
     }
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-        {
-            mn[a] = fminf(mn[a], __shfl_xor_sync(0xffffffffu, mn[a], o));
-            mx[a] = fmaxf(mx[a], __shfl_xor_sync(0xffffffffu, mx[a], o));
-        }
-    if ((threadIdx.x & 31) == 0 && n > 0)
-        for (int a = 0; a < 3; ++a)
-        {
-            atomicMin(ord + 6 * seg + a, float_to_ordered(mn[a]));
-            atomicMax(ord + 6 * seg + 3 + a, float_to_ordered(mx[a]));
-        }
+    block_bounds_commit(mn, mx, ord + 6 * seg);
 }
 
 // key layout shared by all segments; per-segment origin = unpadded aabb min
@@ -176,20 +165,44 @@ __global__ void k_run_flags(SortBuffers sb, const int32_t *d_n, int32_t *flags)
         flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
 }
 
+// run starts of the sorted keys, and the first run (voxel) of every segment
 __global__ void k_run_starts(const int32_t *flags, const int32_t *vid, const int32_t *d_n, const int32_t *d_m,
-                             int32_t *starts)
+                             int32_t *starts, SortBuffers sb, const KeyLayout *lay, int32_t *seg_first)
 {
     const int n = *d_n;
+    const uint64_t *keys = sb.keys[*sb.d_sel];
+    const KeyLayout L = *lay;
+    const int segshift = L.bx + L.by + L.bz;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        if (flags[i])
-            starts[vid[i]] = i;
+    {
+        if (!flags[i])
+            continue;
+        starts[vid[i]] = i;
+        const int seg = L.bseg ? (int)(keys[i] >> segshift) : 0;
+        if (i == 0 || (L.bseg && (int)(keys[i - 1] >> segshift) != seg))
+            seg_first[seg] = vid[i];
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0)
         starts[*d_m] = n;
 }
 
+// segment offsets of the output; empty segments start where the next one does
+__global__ void k_seg_first_to_offsets(const int32_t *seg_first, int P, const int32_t *d_m, int32_t *off)
+{
+    if (threadIdx.x != 0)
+        return;
+    int32_t next = *d_m;
+    off[P] = next;
+    for (int s = P - 1; s >= 0; --s)
+    {
+        if (seg_first[s] >= 0)
+            next = seg_first[s];
+        off[s] = next;
+    }
+}
+
 __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuffers sb, const int32_t *starts,
-                               const int32_t *d_m, const KeyLayout *lay, float4 *opos, float4 *ocol,
-                               int32_t *seg_count)
+                               const int32_t *d_m, const KeyLayout *lay, float4 *opos, float4 *ocol)
 {
     const int m = *d_m;
     const uint64_t *keys = sb.keys[*sb.d_sel];
@@ -223,22 +236,6 @@ __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuf
         const float r = __fmul_rn(cr, inv), gg = __fmul_rn(cg, inv), b = __fmul_rn(cb, inv);
         opos[v] = make_float4(__fdiv_rn(sx, fn), __fdiv_rn(sy, fn), __fdiv_rn(sz, fn), intensity_of(r, gg, b));
         ocol[v] = make_float4(r, gg, b, 0.0f);
-        atomicAdd(seg_count + seg, 1);
-    }
-}
-
-// offsets from per-segment counts (one block)
-__global__ void k_counts_to_offsets(const int32_t *count, int P, int32_t *off)
-{
-    if (threadIdx.x == 0)
-    {
-        int32_t s = 0;
-        for (int i = 0; i < P; ++i)
-        {
-            off[i] = s;
-            s += count[i];
-        }
-        off[P] = s;
     }
 }
 
@@ -295,15 +292,14 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     st = exclusive_scan(ctx, flags, vid, d_n, total_cap, d_m);
     if (st)
         return st;
-    k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts);
+    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0xFF, sizeof(int32_t) * P, s));
+    k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts, sb, lay, seg_count);
     GCA_CHECK_LAUNCH(ctx);
-    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0, sizeof(int32_t) * P, s));
     GCA_PROF_BEGIN(ctx, kKidVoxelReduce);
-    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col,
-                                         seg_count);
+    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidVoxelReduce);
-    k_counts_to_offsets<<<1, 32, 0, s>>>(seg_count, P, out.seg_off);
+    k_seg_first_to_offsets<<<1, 32, 0, s>>>(seg_count, P, d_m, out.seg_off);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
