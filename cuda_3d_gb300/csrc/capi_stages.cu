@@ -10,22 +10,6 @@ using namespace gca3d;
 namespace
 {
 
-// a single-segment batch view of a cloud (no copy)
-int cloud_batch(gca3d_context *ctx, gca3d_cloud *c, Batch &b)
-{
-    b.pos = c->pos;
-    b.col = c->col;
-    b.nrm = c->nrm;
-    b.grd = c->grd;
-    b.P = 1;
-    b.cap = c->capacity;
-    b.max_seg_cap = c->capacity;
-    b.seg_off = ctx->arena.get<int32_t>(2);
-    if (!b.seg_off)
-        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "cloud_batch: scratch");
-    return single_seg_offsets(ctx, c->d_count, b.seg_off);
-}
-
 __global__ void k_set_count(const int32_t *src, int32_t *dst)
 {
     *dst = *src;
@@ -50,6 +34,22 @@ int upload_segsrc(gca3d_context *ctx, gca3d_cloud *const *clouds, int P, SegSrc 
 
 namespace gca3d
 {
+// a single-segment batch view of a cloud (no copy)
+int cloud_batch(gca3d_context *ctx, gca3d_cloud *c, Batch &b)
+{
+    b.pos = c->pos;
+    b.col = c->col;
+    b.nrm = c->nrm;
+    b.grd = c->grd;
+    b.P = 1;
+    b.cap = c->capacity;
+    b.max_seg_cap = c->capacity;
+    b.seg_off = ctx->arena.get<int32_t>(2);
+    if (!b.seg_off)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "cloud_batch: scratch");
+    return single_seg_offsets(ctx, c->d_count, b.seg_off);
+}
+
 int make_segsrc(gca3d_context *ctx, gca3d_cloud *const *clouds, int P, SegSrc **out)
 {
     return upload_segsrc(ctx, clouds, P, out);

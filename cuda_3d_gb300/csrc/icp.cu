@@ -21,206 +21,13 @@
 // cloud is never rewritten: the pose is applied on the fly.
 #include "grid_query.cuh"
 #include "icp.cuh"
+#include "pose_math.cuh"
 #include "stages.cuh"
 
 #include <algorithm>
 
 namespace gca3d
 {
-
-// ---------------------------------------------------------------------------
-// FP64 6x6 solve and pose maps (device; the oracle restates the same steps)
-// ---------------------------------------------------------------------------
-__device__ int solve6_device(const double *S /* 21 upper + 6 rhs */, double x[6])
-{
-    double A[6][6], b[6], D[6];
-    int perm[6];
-    int status = 0;
-    int u = 0;
-    for (int i = 0; i < 6; ++i)
-        for (int j = i; j < 6; ++j)
-        {
-            A[i][j] = A[j][i] = S[u];
-            ++u;
-        }
-    for (int i = 0; i < 6; ++i)
-    {
-        b[i] = -S[21 + i];
-        perm[i] = i;
-    }
-    for (int i = 0; i < 6; ++i)
-    {
-        if (!isfinite(b[i]))
-            status = 1;
-        for (int j = 0; j < 6; ++j)
-            if (!isfinite(A[i][j]))
-                status = 1;
-    }
-    if (status)
-    {
-        for (int i = 0; i < 6; ++i)
-            x[i] = 0.0;
-        return 1;
-    }
-    for (int k = 0; k < 6; ++k)
-    {
-        int piv = k;
-        for (int i = k + 1; i < 6; ++i)
-            if (fabs(A[i][i]) > fabs(A[piv][piv]))
-                piv = i;
-        if (piv != k)
-        {
-            for (int j = 0; j < 6; ++j)
-            {
-                double t = A[k][j];
-                A[k][j] = A[piv][j];
-                A[piv][j] = t;
-            }
-            for (int i = 0; i < 6; ++i)
-            {
-                double t = A[i][k];
-                A[i][k] = A[i][piv];
-                A[i][piv] = t;
-            }
-            int t = perm[k];
-            perm[k] = perm[piv];
-            perm[piv] = t;
-        }
-        D[k] = A[k][k];
-        if (fabs(D[k]) <= 2.2250738585072014e-308)
-        {
-            status = 1;
-            for (int i = k + 1; i < 6; ++i)
-                A[i][k] = 0.0;
-            continue;
-        }
-        for (int i = k + 1; i < 6; ++i)
-            A[i][k] /= D[k];
-        for (int i = k + 1; i < 6; ++i)
-            for (int j = k + 1; j <= i; ++j)
-            {
-                A[i][j] -= A[i][k] * A[j][k] * D[k];
-                A[j][i] = A[i][j];
-            }
-    }
-    double y[6], z[6];
-    for (int i = 0; i < 6; ++i)
-    {
-        double s = b[perm[i]];
-        for (int j = 0; j < i; ++j)
-            s -= A[i][j] * y[j];
-        y[i] = s;
-    }
-    for (int i = 0; i < 6; ++i)
-        y[i] = fabs(D[i]) > 2.2250738585072014e-308 ? y[i] / D[i] : 0.0;
-    for (int i = 5; i >= 0; --i)
-    {
-        double s = y[i];
-        for (int j = i + 1; j < 6; ++j)
-            s -= A[j][i] * z[j];
-        z[i] = s;
-    }
-    for (int i = 0; i < 6; ++i)
-        x[perm[i]] = z[i];
-    return status;
-}
-
-__device__ void pose_from_x_device(const double x[6], int map, double T[16])
-{
-    double R[3][3], t[3];
-    if (map == GCA3D_UPDATE_EULER_ZYX)
-    {
-        double sa, ca, sb, cb, sc, cc;
-        sincos(x[0], &sa, &ca);
-        sincos(x[1], &sb, &cb);
-        sincos(x[2], &sc, &cc);
-        R[0][0] = cc * cb;
-        R[0][1] = cc * sb * sa - sc * ca;
-        R[0][2] = cc * sb * ca + sc * sa;
-        R[1][0] = sc * cb;
-        R[1][1] = sc * sb * sa + cc * ca;
-        R[1][2] = sc * sb * ca - cc * sa;
-        R[2][0] = -sb;
-        R[2][1] = cb * sa;
-        R[2][2] = cb * ca;
-        t[0] = x[3], t[1] = x[4], t[2] = x[5];
-    }
-    else
-    {
-        const double w0 = x[0], w1 = x[1], w2 = x[2];
-        const double th2 = w0 * w0 + w1 * w1 + w2 * w2, th = sqrt(th2);
-        double A, B, C;
-        if (th < 1e-4)
-        {
-            A = 1.0 - th2 / 6.0 + th2 * th2 / 120.0;
-            B = 0.5 - th2 / 24.0 + th2 * th2 / 720.0;
-            C = 1.0 / 6.0 - th2 / 120.0 + th2 * th2 / 5040.0;
-        }
-        else
-        {
-            double s, c;
-            sincos(th, &s, &c);
-            A = s / th;
-            B = (1.0 - c) / th2;
-            C = (th - s) / (th2 * th);
-        }
-        const double K[3][3] = {{0, -w2, w1}, {w2, 0, -w0}, {-w1, w0, 0}};
-        double V[3][3];
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j)
-            {
-                double k2 = K[i][0] * K[0][j] + K[i][1] * K[1][j] + K[i][2] * K[2][j];
-                double I = i == j ? 1.0 : 0.0;
-                R[i][j] = I + A * K[i][j] + B * k2;
-                V[i][j] = I + B * K[i][j] + C * k2;
-            }
-        for (int i = 0; i < 3; ++i)
-            t[i] = V[i][0] * x[3] + V[i][1] * x[4] + V[i][2] * x[5];
-    }
-    for (int i = 0; i < 3; ++i)
-    {
-        for (int j = 0; j < 3; ++j)
-            T[4 * i + j] = R[i][j];
-        T[4 * i + 3] = t[i];
-    }
-    T[12] = T[13] = T[14] = 0.0;
-    T[15] = 1.0;
-}
-
-// ---------------------------------------------------------------------------
-// per-correspondence terms (cuda_color_icp_build_least_square.cu:184-253)
-// ---------------------------------------------------------------------------
-struct GNTerms
-{
-    float Jg[6], Jc[6];
-    float rg, rc;
-};
-
-__device__ __forceinline__ void gn_terms(float3 p, float Is, float3 q, float Iq, float3 n, float3 d, float slg,
-                                         float slc, GNTerms &o)
-{
-    const float rg_ = (p.x - q.x) * n.x + (p.y - q.y) * n.y + (p.z - q.z) * n.z;
-    o.Jg[0] = slg * (p.y * n.z - p.z * n.y);
-    o.Jg[1] = slg * (p.z * n.x - p.x * n.z);
-    o.Jg[2] = slg * (p.x * n.y - p.y * n.x);
-    o.Jg[3] = slg * n.x;
-    o.Jg[4] = slg * n.y;
-    o.Jg[5] = slg * n.z;
-    o.rg = slg * rg_;
-    // d^T (I - n n^T)
-    const float nd = n.x * d.x + n.y * d.y + n.z * d.z;
-    const float tx = d.x - nd * n.x, ty = d.y - nd * n.y, tz = d.z - nd * n.z;
-    o.Jc[0] = slc * (p.y * tz - p.z * ty);
-    o.Jc[1] = slc * (p.z * tx - p.x * tz);
-    o.Jc[2] = slc * (p.x * ty - p.y * tx);
-    o.Jc[3] = slc * tx;
-    o.Jc[4] = slc * ty;
-    o.Jc[5] = slc * tz;
-    // photometric residual on the tangent plane
-    const float px = p.x - rg_ * n.x, py = p.y - rg_ * n.y, pz = p.z - rg_ * n.z;
-    const float Iproj = Iq + (d.x * (px - q.x) + d.y * (py - q.y) + d.z * (pz - q.z));
-    o.rc = slc * (Iproj - Is);
-}
 
 // accumulator of kTerms values: plain FP32 or FP32 value + FP32 error (two-sum)
 template <bool Comp> struct Acc
@@ -431,12 +238,6 @@ __device__ __forceinline__ BlockPair block_pair(const int32_t *src_off, const Pa
     return b;
 }
 
-__device__ __forceinline__ float3 apply_pose(const float *T, float4 s)
-{
-    return make_float3(T[0] * s.x + T[1] * s.y + T[2] * s.z + T[3], T[4] * s.x + T[5] * s.y + T[6] * s.z + T[7],
-                       T[8] * s.x + T[9] * s.y + T[10] * s.z + T[11]);
-}
-
 // step 1 of an iteration: the correspondence of every active source point
 // (grid position and squared distance, -1 when none within max_corr)
 __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
@@ -556,6 +357,17 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restr
         Ps.inlier_rmse = S[28] > 0.0 ? sqrt(S[29] / S[28]) : 0.0;
         double x[6], Ti[16];
         const int singular = solve6_device(S, x);
+        if (prm.trace && Ps.iters < prm.trace_cap)
+        {
+            IcpTrace &tr = prm.trace[(size_t)Ps.iters * P + pair];
+            for (int k = 0; k < 16; ++k)
+                tr.T[k] = Ps.T[k];
+            for (int k = 0; k < kTerms; ++k)
+                tr.S[k] = S[k];
+            for (int k = 0; k < 6; ++k)
+                tr.x[k] = x[k];
+            tr.status = singular;
+        }
         if (S[28] == 0.0)
             Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
         else if (singular && Ps.status == 0)

@@ -30,12 +30,25 @@ struct PairState
     int scale_ntgt[GCA3D_MAX_SCALES];
 };
 
+// what the finalize of an iteration saw: the pose it started from, the summed
+// system and the step (recorded for the adjoint of unrolled iterations)
+struct IcpTrace
+{
+    double T[16];
+    double S[kTerms];
+    double x[6];
+    int status;
+    int pad;
+};
+
 struct IcpScale
 {
     float max_corr;
     float sqrt_lg, sqrt_lc;
     int update_map;
     double rot_eps, trans_eps;
+    IcpTrace *trace = nullptr; // [trace_cap iterations][P pairs] or null
+    int trace_cap = 0;
 };
 
 // the Gauss-Newton system for given correspondences (defined in icp.cu); the block

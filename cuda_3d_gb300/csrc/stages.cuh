@@ -50,6 +50,9 @@ int seg_bounds(gca3d_context *ctx, const float4 *pos, const int32_t *seg_off, in
                int *ord);
 int single_seg_offsets(gca3d_context *ctx, const int32_t *d_n, int32_t *seg_off);
 
+// a single-segment batch view of a cloud (no copy; segment offsets from the arena)
+int cloud_batch(gca3d_context *ctx, gca3d_cloud *c, Batch &b);
+
 // allocate a batch from the context arena
 int batch_alloc(gca3d_context *ctx, Batch &b, int P, int64_t cap, int64_t max_seg_cap, bool nrm, bool grd);
 

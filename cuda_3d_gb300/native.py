@@ -61,6 +61,10 @@ class IcpResult(C.Structure):
                 ("scale_n_tgt", C.c_int * MAX_SCALES)]
 
 
+class VjpParams(C.Structure):
+    _fields_ = [("K", C.c_int), ("max_corr", C.c_float), ("lambda_", C.c_float), ("update_map", C.c_int)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _F = C.c_float
@@ -107,6 +111,8 @@ _SIGS = {
     "gca3d_icp_plan_execute": [_P, _P, _P],
     "gca3d_icp_plan_destroy": [_P],
     "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
+    "gca3d_color_icp_vjp": [_P, _P, _P, C.POINTER(VjpParams), _P, _P, C.c_double, _P, C.POINTER(C.c_double), _P,
+                            _P, _P, _P],
 }
 _RESTYPES = {"gca3d_status_string": C.c_char_p, "gca3d_last_error": C.c_char_p,
              "gca3d_kernel_launches": C.c_int64, "gca3d_stream": C.c_void_p}
@@ -357,3 +363,41 @@ def color_icp_batched(ctx, srcs, tgts, params, T_init=None):
     ctx.check(ctx.L.gca3d_color_icp_batched(ctx.h, P, cloud_array(srcs), cloud_array(tgts), C.byref(params),
                                             _ptr(Ti), res))
     return [result_dict(r) for r in res]
+
+
+def color_icp_vjp(ctx, src, tgt, xi0, K=5, max_corr=0.05, lam=0.968, update_map=UPDATE_SE3_EXP, dT=None, dE=0.0,
+                  n_src=None, want_corr=False, out=None):
+    """K unrolled Gauss-Newton steps from Exp(xi0) and, when dT is given, the gradient of
+    <dT, T_K> + dE * E.  Returns a dict with T (4x4), E and, with dT, dxi0 (6),
+    dxyz / drgb (n_src x 3, host arrays unless `out` supplies device buffers
+    {"dxyz", "drgb"}), plus corr ((K + 1) x n_src) when want_corr."""
+    p = VjpParams(int(K), float(max_corr), float(lam), int(update_map))
+    n = len(src) if n_src is None else int(n_src)
+    x0 = np.ascontiguousarray(np.asarray(xi0, np.float64).reshape(6))
+    T = np.zeros(16, np.float64)
+    E = C.c_double()
+    res = {}
+    dxi = np.zeros(6, np.float64)
+    gT = None if dT is None else np.ascontiguousarray(np.asarray(dT, np.float64).reshape(16))
+    own = out is None and dT is not None
+    bx = by = None
+    if dT is not None:
+        bx = ctx.alloc(12 * max(n, 1)) if own else out["dxyz"]
+        by = ctx.alloc(12 * max(n, 1)) if own else out["drgb"]
+    bc = ctx.alloc(4 * (K + 1) * max(n, 1)) if want_corr else None
+    st = ctx.L.gca3d_color_icp_vjp(ctx.h, src.h, tgt.h, C.byref(p), _ptr(x0), _ptr(gT), float(dE), _ptr(T),
+                                   C.byref(E), _ptr(dxi) if dT is not None else None, bx.ptr if bx else None,
+                                   by.ptr if by else None, bc.ptr if bc else None)
+    res["status"] = st
+    if st not in (OK, ERR_SINGULAR):
+        ctx.check(st)
+    res["T"] = T.reshape(4, 4)
+    res["E"] = E.value
+    if dT is not None:
+        res["dxi0"] = dxi
+        if own:
+            res["dxyz"] = bx.read(np.float32, 3 * n).reshape(n, 3)
+            res["drgb"] = by.read(np.float32, 3 * n).reshape(n, 3)
+    if want_corr:
+        res["corr"] = bc.read(np.int32, (K + 1) * n).reshape(K + 1, n)
+    return res

@@ -275,6 +275,32 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *plan);
 /* kernels one execute launches (graph nodes, or the eager launches of the last run) */
 int gca3d_icp_plan_kernels(gca3d_icp_plan *plan, int64_t *n);
 
+/* ---------------------------------------------------------------------------
+ * adjoint of K unrolled Gauss-Newton steps (no reference counterpart)
+ * ------------------------------------------------------------------------- */
+#define GCA3D_VJP_MAX_STEPS 64
+typedef struct gca3d_vjp_params {
+    int K;          /* Gauss-Newton steps, 1..GCA3D_VJP_MAX_STEPS */
+    float max_corr; /* correspondence distance (m) */
+    float lambda;   /* weight of the geometric term, [0, 1] */
+    int update_map; /* GCA3D_UPDATE_* */
+} gca3d_vjp_params;
+
+/* K colored-ICP Gauss-Newton steps of one pair from T_0 = Exp(xi0) (SE(3)
+ * exponential, xi = (w, v)), no convergence test, and -- when dT is not NULL -- the
+ * gradient of L = <dT, T_K> (rows 0-2 of the row-major 4x4) + dE * E with respect
+ * to xi0, the source points and the source colours, correspondences held fixed
+ * (they are piecewise constant).  E is the sum of the weighted r_g^2 + r_c^2 at T_K.
+ * The target needs normals and colour gradients (gca3d_estimate_normals,
+ * gca3d_color_gradient).  T_out, E_out: may be NULL.  d_dxyz, d_drgb: device
+ * float[n_src * 3].  d_corr (may be NULL): device int32[(K + 1) * n_src], the
+ * target index of every source point at every evaluation (-1: none).
+ * Returns GCA3D_ERR_SINGULAR (outputs written) when a step's system was singular. */
+int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt,
+                        const gca3d_vjp_params *params, const double xi0[6], const double dT[16],
+                        double dE, double T_out[16], double *E_out, double dxi0[6], float *d_dxyz,
+                        float *d_drgb, int32_t *d_corr);
+
 #ifdef __cplusplus
 }
 #endif

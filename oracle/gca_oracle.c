@@ -1441,3 +1441,433 @@ void orc_color_icp_ref32(const float *sx_in, const float *srgb, int64_t ns, cons
     free(sx);
     free(nn);
 }
+
+/* ------------------------------------------------------------------ */
+/* a21: K unrolled Gauss-Newton steps of the colored-ICP objective and  */
+/* their adjoint (no reference counterpart; FP64).  The per-point rows  */
+/* follow compute_JTJ_JTr_and_r_gauss_newton_functor                    */
+/* (cuda_color_icp_build_least_square.cu:184-253); the step follows     */
+/* solve_JTJ_JTr (eigen_solver.hpp:44-85) with the chosen pose map.     */
+/* ------------------------------------------------------------------ */
+
+/* d U(x) / d x_m as 3x4 row-major blocks, for both pose maps */
+void orc_pose_jacobian(const double x[6], int update_map, double dU[6][12])
+{
+    memset(dU, 0, sizeof(double) * 72);
+    if (update_map == ORC_UPDATE_EULER_ZYX) {
+        double ca = cos(x[0]), sa = sin(x[0]), cb = cos(x[1]), sb = sin(x[1]);
+        double cc = cos(x[2]), sc = sin(x[2]);
+        double Rx[9] = {1, 0, 0, 0, ca, -sa, 0, sa, ca}, dRx[9] = {0, 0, 0, 0, -sa, -ca, 0, ca, -sa};
+        double Ry[9] = {cb, 0, sb, 0, 1, 0, -sb, 0, cb}, dRy[9] = {-sb, 0, cb, 0, 0, 0, -cb, 0, -sb};
+        double Rz[9] = {cc, -sc, 0, sc, cc, 0, 0, 0, 1}, dRz[9] = {-sc, -cc, 0, cc, -sc, 0, 0, 0, 0};
+        const double *f[3][3] = {{Rz, Ry, dRx}, {Rz, dRy, Rx}, {dRz, Ry, Rx}};
+        for (int m = 0; m < 3; ++m) {
+            double M1[9], M2[9];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double s = 0;
+                    for (int k = 0; k < 3; ++k)
+                        s += f[m][0][3 * i + k] * f[m][1][3 * k + j];
+                    M1[3 * i + j] = s;
+                }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double s = 0;
+                    for (int k = 0; k < 3; ++k)
+                        s += M1[3 * i + k] * f[m][2][3 * k + j];
+                    M2[3 * i + j] = s;
+                }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                    dU[m][4 * i + j] = M2[3 * i + j];
+        }
+        for (int i = 0; i < 3; ++i)
+            dU[3 + i][4 * i + 3] = 1.0;
+        return;
+    }
+    /* SE(3) exponential: R = I + A K + B K^2, t = (I + B K + C K^2) v with
+     * K = [w]x; A, B, C and their derivatives with respect to theta^2 */
+    double w[3] = {x[0], x[1], x[2]}, v[3] = {x[3], x[4], x[5]};
+    double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2], th = sqrt(th2);
+    double A, B, C, Ad, Bd, Cd;
+    if (th < 1e-2) {
+        double t4 = th2 * th2, t6 = t4 * th2;
+        A = 1.0 - th2 / 6.0 + t4 / 120.0 - t6 / 5040.0;
+        B = 0.5 - th2 / 24.0 + t4 / 720.0 - t6 / 40320.0;
+        C = 1.0 / 6.0 - th2 / 120.0 + t4 / 5040.0 - t6 / 362880.0;
+        Ad = -1.0 / 6.0 + th2 / 60.0 - t4 / 1680.0;
+        Bd = -1.0 / 24.0 + th2 / 360.0 - t4 / 13440.0;
+        Cd = -1.0 / 120.0 + th2 / 2520.0 - t4 / 120960.0;
+    } else {
+        double s = sin(th), c = cos(th);
+        A = s / th;
+        B = (1.0 - c) / th2;
+        C = (th - s) / (th2 * th);
+        Ad = (th * c - s) / (2.0 * th2 * th);
+        Bd = (th * s - 2.0 * (1.0 - c)) / (2.0 * th2 * th2);
+        Cd = ((1.0 - c) * th - 3.0 * (th - s)) / (2.0 * th2 * th2 * th);
+    }
+    double K[3][3] = {{0, -w[2], w[1]}, {w[2], 0, -w[0]}, {-w[1], w[0], 0}};
+    double K2[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0;
+            for (int k = 0; k < 3; ++k)
+                s += K[i][k] * K[k][j];
+            K2[i][j] = s;
+        }
+    for (int m = 0; m < 3; ++m) {
+        double G[3][3] = {{0}};
+        /* [e_m]x */
+        if (m == 0) { G[1][2] = -1; G[2][1] = 1; }
+        if (m == 1) { G[0][2] = 1; G[2][0] = -1; }
+        if (m == 2) { G[0][1] = -1; G[1][0] = 1; }
+        double GK[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double s = 0;
+                for (int k = 0; k < 3; ++k)
+                    s += G[i][k] * K[k][j] + K[i][k] * G[k][j];
+                GK[i][j] = s;
+            }
+        double dR[3][3], dV[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                dR[i][j] = 2.0 * w[m] * Ad * K[i][j] + A * G[i][j] + 2.0 * w[m] * Bd * K2[i][j] + B * GK[i][j];
+                dV[i][j] = 2.0 * w[m] * Bd * K[i][j] + B * G[i][j] + 2.0 * w[m] * Cd * K2[i][j] + C * GK[i][j];
+            }
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j)
+                dU[m][4 * i + j] = dR[i][j];
+            dU[m][4 * i + 3] = dV[i][0] * v[0] + dV[i][1] * v[1] + dV[i][2] * v[2];
+        }
+    }
+    for (int m = 0; m < 3; ++m)
+        for (int i = 0; i < 3; ++i)
+            dU[3 + m][4 * i + 3] = (i == m ? 1.0 : 0.0) + B * K[i][m] + C * K2[i][m];
+}
+
+/* the two weighted rows of one correspondence (FP64) */
+typedef struct {
+    double Jg[6], Jc[6], rg, rc;
+    d3 n, dt; /* normal and the tangential colour gradient (I - n n^T) d */
+} orc_rows;
+
+static void rows_f64(d3 p, double Is, d3 q, double Iq, d3 n, d3 d, double slg, double slc, orc_rows *o)
+{
+    double rg = d3dot(d3sub(p, q), n);
+    double nd = d3dot(n, d);
+    d3 dt = d3m(d.x - nd * n.x, d.y - nd * n.y, d.z - nd * n.z);
+    d3 a1 = d3cross(p, n), a2 = d3cross(p, dt);
+    double Jg[6] = {a1.x, a1.y, a1.z, n.x, n.y, n.z};
+    double Jc[6] = {a2.x, a2.y, a2.z, dt.x, dt.y, dt.z};
+    for (int k = 0; k < 6; ++k) {
+        o->Jg[k] = slg * Jg[k];
+        o->Jc[k] = slc * Jc[k];
+    }
+    o->rg = slg * rg;
+    o->rc = slc * (Iq + d3dot(dt, d3sub(p, q)) - Is);
+    o->n = n;
+    o->dt = dt;
+}
+
+typedef struct {
+    const double *sx, *srgb;
+    int64_t ns;
+    const float *tx;
+    const double *tn, *tg;
+    double *It;
+    int64_t nt;
+    double slg, slc;
+    float gmin[3];
+    double cell, rr;
+    ogrid g; /* FP64 cell coordinates, (distance, index) tie-break */
+} unroll_ctx;
+
+static d3 pose_apply(const double T[16], d3 s)
+{
+    return d3m(T[0] * s.x + T[1] * s.y + T[2] * s.z + T[3], T[4] * s.x + T[5] * s.y + T[6] * s.z + T[7],
+               T[8] * s.x + T[9] * s.y + T[10] * s.z + T[11]);
+}
+
+static int64_t nn_f64(const unroll_ctx *u, d3 p)
+{
+    int32_t c[3];
+    c[0] = (int32_t)floor((p.x - (double)u->gmin[0]) / u->cell);
+    c[1] = (int32_t)floor((p.y - (double)u->gmin[1]) / u->cell);
+    c[2] = (int32_t)floor((p.z - (double)u->gmin[2]) / u->cell);
+    double best = u->rr;
+    int64_t bi = -1;
+    for (int di = -1; di <= 1; ++di)
+        for (int dj = -1; dj <= 1; ++dj)
+            for (int dk = -1; dk <= 1; ++dk) {
+                int32_t x = c[0] + di, y = c[1] + dj, z = c[2] + dk;
+                for (int64_t s = grid_lower(&u->g, x, y, z); s < u->g.n; ++s) {
+                    const vkey *e = &u->g.cells[s];
+                    if (e->k[0] != x || e->k[1] != y || e->k[2] != z)
+                        break;
+                    d3 dd = d3sub(d3loadf(u->tx, e->idx), p);
+                    double d2 = d3dot(dd, dd);
+                    if (d2 < u->rr && (bi < 0 || d2 < best || (d2 == best && e->idx < bi))) {
+                        best = d2;
+                        bi = e->idx;
+                    }
+                }
+            }
+    return bi;
+}
+
+static void unroll_open(unroll_ctx *u, const double *sx, const double *srgb, int64_t ns, const float *tx,
+                        const float *trgb, const double *tn, const double *tg, int64_t nt,
+                        const orc_unroll_params *p, int need_grid)
+{
+    memset(u, 0, sizeof *u);
+    u->sx = sx, u->srgb = srgb, u->ns = ns, u->tx = tx, u->tn = tn, u->tg = tg, u->nt = nt;
+    u->slg = sqrt((double)p->lambda);
+    u->slc = sqrt(1.0 - (double)p->lambda);
+    u->It = (double *)malloc(sizeof(double) * (size_t)(nt > 0 ? nt : 1));
+    for (int64_t j = 0; j < nt; ++j)
+        u->It[j] = orc_intensity(trgb[3 * j], trgb[3 * j + 1], trgb[3 * j + 2]);
+    u->cell = (double)p->max_corr;
+    u->rr = u->cell * u->cell;
+    if (need_grid && nt > 0) {
+        float amin[3], amax[3];
+        orc_aabb(tx, nt, 0, amin, amax);
+        for (int a = 0; a < 3; ++a)
+            u->gmin[a] = amin[a] - 1.5f * p->max_corr;
+        u->g.n = nt;
+        u->g.cells = (vkey *)malloc(sizeof(vkey) * (size_t)nt);
+        for (int64_t j = 0; j < nt; ++j) {
+            for (int a = 0; a < 3; ++a)
+                u->g.cells[j].k[a] = (int32_t)floor(((double)tx[3 * j + a] - (double)u->gmin[a]) / u->cell);
+            u->g.cells[j].idx = j;
+        }
+        qsort(u->g.cells, (size_t)nt, sizeof(vkey), cmp_vkey);
+    }
+}
+
+static void unroll_close(unroll_ctx *u)
+{
+    free(u->It);
+    free(u->g.cells);
+}
+
+/* source intensity as an exact FP64 function of the colour (smooth in the colour) */
+static const double kIw[3] = {0.2126, 0.7152, 0.0722};
+static double src_intensity(const unroll_ctx *u, int64_t i)
+{
+    return kIw[0] * u->srgb[3 * i] + kIw[1] * u->srgb[3 * i + 1] + kIw[2] * u->srgb[3 * i + 2];
+}
+
+static int corr_rows(const unroll_ctx *u, int64_t i, int64_t j, d3 p, orc_rows *o)
+{
+    if (j < 0 || j >= u->nt)
+        return 0;
+    d3 q = d3loadf(u->tx, j);
+    d3 n = d3m(u->tn[3 * j], u->tn[3 * j + 1], u->tn[3 * j + 2]);
+    d3 d = d3m(u->tg[3 * j], u->tg[3 * j + 1], u->tg[3 * j + 2]);
+    rows_f64(p, src_intensity(u, i), q, u->It[j], n, d, u->slg, u->slc, o);
+    return 1;
+}
+
+/* one evaluation at pose T: correspondences (frozen from cin or searched and
+ * written to cout), system S[28] = 21 upper JTJ + 6 JTr + sum r^2 */
+static void unroll_eval(const unroll_ctx *u, const double T[16], const int32_t *cin, int32_t *cout, double S[28])
+{
+    memset(S, 0, sizeof(double) * 28);
+    for (int64_t i = 0; i < u->ns; ++i) {
+        d3 p = pose_apply(T, d3m(u->sx[3 * i], u->sx[3 * i + 1], u->sx[3 * i + 2]));
+        int64_t j = cin ? cin[i] : nn_f64(u, p);
+        if (cout)
+            cout[i] = (int32_t)j;
+        orc_rows o;
+        if (!corr_rows(u, i, j, p, &o))
+            continue;
+        int k = 0;
+        for (int a = 0; a < 6; ++a)
+            for (int b = a; b < 6; ++b)
+                S[k++] += o.Jg[a] * o.Jg[b] + o.Jc[a] * o.Jc[b];
+        for (int a = 0; a < 6; ++a)
+            S[21 + a] += o.Jg[a] * o.rg + o.Jc[a] * o.rc;
+        S[27] += o.rg * o.rg + o.rc * o.rc;
+    }
+}
+
+static void sys_to_full(const double S[28], double H[36], double b[6])
+{
+    int k = 0;
+    for (int a = 0; a < 6; ++a)
+        for (int c = a; c < 6; ++c) {
+            H[6 * a + c] = H[6 * c + a] = S[k];
+            ++k;
+        }
+    for (int a = 0; a < 6; ++a)
+        b[a] = S[21 + a];
+}
+
+/* forward of the unrolled steps; Ts receives the K + 1 poses, xs the K steps,
+ * Ss the K + 1 systems (each may be NULL) */
+static double unroll_forward(const unroll_ctx *u, const orc_unroll_params *p, const double xi0[6],
+                             const int32_t *cin, int32_t *cout, double *Ts, double *xs, double *Ss, int *status)
+{
+    double T[16], S[28];
+    orc_pose_from_x(xi0, ORC_UPDATE_SE3_EXP, T);
+    *status = 0;
+    for (int k = 0; k <= p->K; ++k) {
+        unroll_eval(u, T, cin ? cin + (size_t)k * u->ns : NULL, cout ? cout + (size_t)k * u->ns : NULL, S);
+        if (Ts)
+            memcpy(Ts + 16 * k, T, sizeof T);
+        if (Ss)
+            memcpy(Ss + 28 * k, S, sizeof S);
+        if (k == p->K)
+            break;
+        double H[36], b[6], x[6], U[16];
+        sys_to_full(S, H, b);
+        if (orc_solve6(H, b, x))
+            *status = 1;
+        if (xs)
+            memcpy(xs + 6 * k, x, sizeof x);
+        orc_pose_from_x(x, p->update_map, U);
+        mat4_mul_d(U, T, T);
+    }
+    return S[27];
+}
+
+double orc_icp_unrolled_f64(const double *sx, const double *srgb, int64_t ns, const float *tx, const float *trgb,
+                            const double *tn, const double *tg, int64_t nt, const orc_unroll_params *p,
+                            const double xi0[6], const int32_t *corr_in, int32_t *corr_out, double T_out[16])
+{
+    unroll_ctx u;
+    unroll_open(&u, sx, srgb, ns, tx, trgb, tn, tg, nt, p, corr_in == NULL);
+    double *Ts = (double *)malloc(sizeof(double) * 16 * (size_t)(p->K + 1));
+    int status;
+    double E = unroll_forward(&u, p, xi0, corr_in, corr_out, Ts, NULL, NULL, &status);
+    if (T_out)
+        memcpy(T_out, Ts + 16 * p->K, sizeof(double) * 16);
+    free(Ts);
+    unroll_close(&u);
+    return E;
+}
+
+/* adjoint of one evaluation at pose T with correspondences c: the rows' adjoints
+ * are  jbar = -y (j.x) - x (j.y) - r y  and  rbar = -(j.y) + 2 e r  (x = y = 0 for
+ * the objective, e = 0 for a step).  Adds to dxyz, drgb and Tbar (3x4). */
+static void unroll_point_adjoint(const unroll_ctx *u, const double T[16], const int32_t *c, const double x[6],
+                                 const double y[6], double e, double *dxyz, double *drgb, double Tbar[12])
+{
+    for (int64_t i = 0; i < u->ns; ++i) {
+        d3 s = d3m(u->sx[3 * i], u->sx[3 * i + 1], u->sx[3 * i + 2]);
+        d3 p = pose_apply(T, s);
+        orc_rows o;
+        if (!corr_rows(u, i, c[i], p, &o))
+            continue;
+        d3 pb = d3m(0, 0, 0);
+        double Ib = 0.0;
+        for (int row = 0; row < 2; ++row) {
+            const double *J = row ? o.Jc : o.Jg;
+            double r = row ? o.rc : o.rg, w = row ? u->slc : u->slg;
+            d3 dir = row ? o.dt : o.n;
+            double jx = 0, jy = 0;
+            for (int a = 0; a < 6; ++a) {
+                jx += J[a] * x[a];
+                jy += J[a] * y[a];
+            }
+            d3 jb = d3m(-y[0] * jx - x[0] * jy - r * y[0], -y[1] * jx - x[1] * jy - r * y[1],
+                        -y[2] * jx - x[2] * jy - r * y[2]);
+            double rb = -jy + 2.0 * e * r;
+            /* J top = w (p x dir): d<jb, p x dir> = <dp, dir x jb> */
+            d3 cr = d3cross(dir, jb);
+            pb = d3m(pb.x + w * cr.x + rb * w * dir.x, pb.y + w * cr.y + rb * w * dir.y,
+                     pb.z + w * cr.z + rb * w * dir.z);
+            if (row)
+                Ib += -rb * w;
+        }
+        /* p = R s + t */
+        dxyz[3 * i + 0] += T[0] * pb.x + T[4] * pb.y + T[8] * pb.z;
+        dxyz[3 * i + 1] += T[1] * pb.x + T[5] * pb.y + T[9] * pb.z;
+        dxyz[3 * i + 2] += T[2] * pb.x + T[6] * pb.y + T[10] * pb.z;
+        for (int a = 0; a < 3; ++a)
+            drgb[3 * i + a] += Ib * kIw[a];
+        double pv[3] = {pb.x, pb.y, pb.z}, sv[3] = {s.x, s.y, s.z};
+        for (int r = 0; r < 3; ++r) {
+            for (int cidx = 0; cidx < 3; ++cidx)
+                Tbar[4 * r + cidx] += pv[r] * sv[cidx];
+            Tbar[4 * r + 3] += pv[r];
+        }
+    }
+}
+
+/* adjoint of T' = U(x) T through the step map and the solve: from Tbar' (3x4)
+ * to xbar, then y = H^-1 xbar; Tbar <- U^T Tbar' (rows 0-2) */
+static int unroll_step_adjoint(const double T[16], const double x[6], const double S[28], int map,
+                               const double Tbar_next[12], double Tbar[12], double y[6])
+{
+    double U[16], dU[6][12], Ub[12], xb[6];
+    orc_pose_from_x(x, map, U);
+    orc_pose_jacobian(x, map, dU);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 4; ++b) {
+            double s = 0;
+            for (int c = 0; c < 4; ++c)
+                s += Tbar_next[4 * a + c] * T[4 * b + c];
+            Ub[4 * a + b] = s;
+        }
+    for (int m = 0; m < 6; ++m) {
+        double s = 0;
+        for (int k = 0; k < 12; ++k)
+            s += Ub[k] * dU[m][k];
+        xb[m] = s;
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 4; ++c) {
+            double s = 0;
+            for (int b = 0; b < 3; ++b)
+                s += U[4 * b + a] * Tbar_next[4 * b + c];
+            Tbar[4 * a + c] = s;
+        }
+    double H[36], bb[6], nxb[6];
+    sys_to_full(S, H, bb);
+    for (int m = 0; m < 6; ++m)
+        nxb[m] = -xb[m];
+    return orc_solve6(H, nxb, y); /* y = -H^-1 (-xbar) */
+}
+
+int orc_icp_unrolled_vjp_f64(const double *sx, const double *srgb, int64_t ns, const float *tx, const float *trgb,
+                             const double *tn, const double *tg, int64_t nt, const orc_unroll_params *p,
+                             const double xi0[6], const int32_t *corr, const double dT[16], double dE,
+                             double dxi0[6], double *dxyz, double *drgb)
+{
+    unroll_ctx u;
+    unroll_open(&u, sx, srgb, ns, tx, trgb, tn, tg, nt, p, 0);
+    const int K = p->K;
+    double *Ts = (double *)malloc(sizeof(double) * 16 * (size_t)(K + 1));
+    double *xs = (double *)malloc(sizeof(double) * 6 * (size_t)(K > 0 ? K : 1));
+    double *Ss = (double *)malloc(sizeof(double) * 28 * (size_t)(K + 1));
+    int status;
+    unroll_forward(&u, p, xi0, corr, NULL, Ts, xs, Ss, &status);
+    memset(dxyz, 0, sizeof(double) * 3 * (size_t)ns);
+    memset(drgb, 0, sizeof(double) * 3 * (size_t)ns);
+    double Tbar[12], Tprev[12], y[6];
+    const double zero6[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 12; ++k)
+        Tbar[k] = dT[k];
+    unroll_point_adjoint(&u, Ts + 16 * K, corr + (size_t)K * ns, zero6, zero6, dE, dxyz, drgb, Tbar);
+    for (int k = K - 1; k >= 0; --k) {
+        status |= unroll_step_adjoint(Ts + 16 * k, xs + 6 * k, Ss + 28 * k, p->update_map, Tbar, Tprev, y);
+        unroll_point_adjoint(&u, Ts + 16 * k, corr + (size_t)k * ns, xs + 6 * k, y, 0.0, dxyz, drgb, Tprev);
+        memcpy(Tbar, Tprev, sizeof Tbar);
+    }
+    double dX[6][12];
+    orc_pose_jacobian(xi0, ORC_UPDATE_SE3_EXP, dX);
+    for (int m = 0; m < 6; ++m) {
+        double s = 0;
+        for (int k = 0; k < 12; ++k)
+            s += Tbar[k] * dX[m][k];
+        dxi0[m] = s;
+    }
+    free(Ts);
+    free(xs);
+    free(Ss);
+    unroll_close(&u);
+    return status;
+}

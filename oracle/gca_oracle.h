@@ -147,6 +147,43 @@ void orc_color_icp_ref32(const float *src_xyz, const float *src_rgb, int64_t ns,
                          const float *tgt_grad, int64_t nt, int max_iter, float max_corr,
                          const float T_init[16], orc_icp_result *res);
 
+/* ------------------------------------------------------------------
+ * K unrolled Gauss-Newton steps of the colored-ICP objective and their
+ * adjoint (no reference counterpart; FP64).  T_0 = Exp(xi0) (SE(3)
+ * exponential, xi = (w, v)); step k solves the system built at T_k and
+ * composes T_{k+1} = U(x_k) T_k with the chosen map; E = sum of the weighted
+ * r_g^2 + r_c^2 at T_K.  Source points and colours are FP64 (finite differences
+ * of the inputs stay exact); the source intensity is the exact FP64 weighted sum.
+ * corr: (K + 1) x ns target indices (-1: none), one row per evaluation; when
+ * given, the correspondences are frozen (the function is then smooth), else they
+ * are searched ((distance, index) minimum within max_corr) and written to
+ * corr_out when it is not NULL.
+ * ------------------------------------------------------------------ */
+typedef struct {
+    int K;
+    float max_corr;
+    float lambda;
+    int update_map;
+} orc_unroll_params;
+
+/* dU/dx_m as 3x4 row-major blocks for U = pose map(x) */
+void orc_pose_jacobian(const double x[6], int update_map, double dU[6][12]);
+
+/* returns E; T_out receives T_K */
+double orc_icp_unrolled_f64(const double *sx, const double *srgb, int64_t ns, const float *tx,
+                            const float *trgb, const double *tn, const double *tg, int64_t nt,
+                            const orc_unroll_params *p, const double xi0[6], const int32_t *corr_in,
+                            int32_t *corr_out, double T_out[16]);
+
+/* gradient of L = <dT, T_K> (rows 0-2) + dE * E with respect to xi0, the source
+ * points and the source colours, correspondences frozen to corr.  Returns nonzero
+ * when a step's system was singular. */
+int orc_icp_unrolled_vjp_f64(const double *sx, const double *srgb, int64_t ns, const float *tx,
+                             const float *trgb, const double *tn, const double *tg, int64_t nt,
+                             const orc_unroll_params *p, const double xi0[6], const int32_t *corr,
+                             const double dT[16], double dE, double dxi0[6], double *dxyz,
+                             double *drgb);
+
 #ifdef __cplusplus
 }
 #endif

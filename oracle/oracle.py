@@ -58,6 +58,10 @@ class IcpParams(C.Structure):
                 ("update_map", C.c_int), ("rot_eps", C.c_double), ("trans_eps", C.c_double)]
 
 
+class UnrollParams(C.Structure):
+    _fields_ = [("K", C.c_int), ("max_corr", C.c_float), ("lambda_", C.c_float), ("update_map", C.c_int)]
+
+
 class IcpResult(C.Structure):
     _fields_ = [("T", C.c_double * 16), ("rmse_ref", C.c_double), ("fitness", C.c_double),
                 ("inlier_rmse", C.c_double), ("iterations", C.c_int), ("converged", C.c_int),
@@ -92,6 +96,12 @@ def _bind(L):
                                   F64, C.POINTER(IcpResult)]),
         "orc_color_icp_ref32": (v, [F32, F32, i64, F32, F32, F32, F32, i64, C.c_int, C.c_float,
                                     F32, C.POINTER(IcpResult)]),
+        "orc_pose_jacobian": (v, [F64, C.c_int, F64]),
+        "orc_icp_unrolled_f64": (C.c_double, [F64, F64, i64, F32, F32, F64, F64, i64,
+                                              C.POINTER(UnrollParams), F64, C.c_void_p, C.c_void_p, F64]),
+        "orc_icp_unrolled_vjp_f64": (C.c_int, [F64, F64, i64, F32, F32, F64, F64, i64,
+                                               C.POINTER(UnrollParams), F64, I32, F64, C.c_double, F64, F64,
+                                               F64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -336,3 +346,50 @@ def multiscale_ref32(src_xyz, src_rgb, tgt_xyz, tgt_rgb, scales, T_init=None):
         T = r.T.astype(np.float32)
         results.append(r)
     return T.astype(np.float64), results
+
+
+# --------------------------------------------------------------------------- #
+# K unrolled Gauss-Newton steps and their adjoint (FP64; no reference
+# counterpart).  T_0 = Exp(xi0); corr is (K + 1) x ns target indices.
+# --------------------------------------------------------------------------- #
+def pose_jacobian(x, update_map=UPDATE_SE3_EXP):
+    d = np.zeros(72, np.float64)
+    lib().orc_pose_jacobian(np.ascontiguousarray(x, np.float64), int(update_map), d)
+    return d.reshape(6, 3, 4)
+
+
+def _unroll_args(src_xyz, src_rgb, tgt_xyz, tgt_rgb, tgt_nrm, tgt_grad):
+    return (np.ascontiguousarray(src_xyz, np.float64).reshape(-1, 3),
+            np.ascontiguousarray(src_rgb, np.float64).reshape(-1, 3), len(src_xyz), _f32(tgt_xyz), _f32(tgt_rgb),
+            np.ascontiguousarray(tgt_nrm, np.float64).reshape(-1, 3),
+            np.ascontiguousarray(tgt_grad, np.float64).reshape(-1, 3), len(tgt_xyz))
+
+
+def icp_unrolled_f64(src_xyz, src_rgb, tgt_xyz, tgt_rgb, tgt_nrm, tgt_grad, xi0, K=5, max_corr=0.05, lam=0.968,
+                     update_map=UPDATE_SE3_EXP, corr=None):
+    """Returns (T_K, E, corr); corr is searched when not given (then returned)."""
+    a = _unroll_args(src_xyz, src_rgb, tgt_xyz, tgt_rgb, tgt_nrm, tgt_grad)
+    p = UnrollParams(int(K), float(max_corr), float(lam), int(update_map))
+    T = np.zeros(16, np.float64)
+    cout = None
+    if corr is None:
+        cout = np.zeros((K + 1, len(src_xyz)), np.int32)
+        cin_p, cout_p = None, cout.ctypes.data
+    else:
+        corr = np.ascontiguousarray(corr, np.int32)
+        cin_p, cout_p = corr.ctypes.data, None
+    E = lib().orc_icp_unrolled_f64(*a, C.byref(p), np.ascontiguousarray(xi0, np.float64), cin_p, cout_p, T)
+    return T.reshape(4, 4), E, (corr if cout is None else cout)
+
+
+def icp_unrolled_vjp_f64(src_xyz, src_rgb, tgt_xyz, tgt_rgb, tgt_nrm, tgt_grad, xi0, corr, dT, dE, K=5,
+                         max_corr=0.05, lam=0.968, update_map=UPDATE_SE3_EXP):
+    """Gradient of <dT, T_K> + dE * E: returns (dxi0, dxyz, drgb, status)."""
+    a = _unroll_args(src_xyz, src_rgb, tgt_xyz, tgt_rgb, tgt_nrm, tgt_grad)
+    p = UnrollParams(int(K), float(max_corr), float(lam), int(update_map))
+    n = len(src_xyz)
+    dxi, dxyz, drgb = np.zeros(6), np.zeros((n, 3)), np.zeros((n, 3))
+    st = lib().orc_icp_unrolled_vjp_f64(*a, C.byref(p), np.ascontiguousarray(xi0, np.float64),
+                                        np.ascontiguousarray(corr, np.int32).reshape(-1),
+                                        np.ascontiguousarray(dT, np.float64).reshape(-1), float(dE), dxi, dxyz, drgb)
+    return dxi, dxyz, drgb, st

@@ -1,0 +1,220 @@
+"""Adjoint of K unrolled colored-ICP Gauss-Newton steps on the GPU (through the C
+ABI) against the FP64 oracle and against FP64 central finite differences.
+
+Workload: a 100k-point pair from the fragment-room generator (10 deg + 10 cm ground
+truth), target normals and colour gradients from the GPU path, K = 5 steps from a
+pose near the ground truth.  The loss is L = <G, T_K> + g * E_K.  The GPU's
+correspondences are handed to the oracle, so both differentiate the same frozen
+function.  Bars:
+  * T_K within 1e-5 rad / 1e-5 m of the oracle's FP64 forward, E_K within 1e-4
+    relative;
+  * point and colour gradients within GRAD_RTOL (normwise over all points) of the
+    FP64 adjoint, the pose gradient within POSE_GRAD_RTOL: the per-point arithmetic
+    is FP32, the cross-block sums FP64 (measured on GB300: 2.4e-5 and 3e-4);
+  * at 64 random coordinates (6 pose, 29 points, 29 colours) the GPU gradient
+    agrees with central differences (h = 1e-4 on the pose, 1e-5 m on points, 1e-4 on
+    colours) within FD_RTOL of the larger of |fd| and 1e-3 of that block's largest
+    gradient;
+  * a torch.autograd.Function around the entry point (test harness only) gives the
+    same gradients through loss.backward()."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+POSE_TOL = 1e-5
+GRAD_RTOL = 1e-4
+POSE_GRAD_RTOL = 2e-3
+FD_RTOL = 2e-3
+MAX_CORR = 0.05
+RADIUS = 0.06
+N_POINTS = 100_000
+
+
+@pytest.fixture(scope="module")
+def N():
+    from cuda_3d_gb300 import build, native
+
+    build.build()
+    return native
+
+
+@pytest.fixture(scope="module")
+def ctx(N):
+    return N.Context(0)
+
+
+def se3_log(T):
+    """(w, v) with Exp(w, v) = T (rotation angle below pi)"""
+    from scipy.spatial.transform import Rotation
+
+    w = Rotation.from_matrix(T[:3, :3]).as_rotvec()
+    th = np.linalg.norm(w)
+    K = np.array([[0, -w[2], w[1]], [w[2], 0, -w[0]], [-w[1], w[0], 0]])
+    B = (1 - np.cos(th)) / th**2 if th > 1e-8 else 0.5
+    Cc = (th - np.sin(th)) / th**3 if th > 1e-8 else 1 / 6
+    V = np.eye(3) + B * K + Cc * K @ K
+    return np.concatenate([w, np.linalg.solve(V, T[:3, 3])])
+
+
+@pytest.fixture(scope="module")
+def c2(ctx, N):
+    from cuda_3d_gb300 import synth
+
+    pr = synth.room_pair(seed=21, n_points=N_POINTS, rot_deg=10.0, trans=0.10)
+    src = ctx.cloud_from(pr.src_xyz, pr.src_rgb)
+    tgt = ctx.cloud_from(pr.tgt_xyz, pr.tgt_rgb)
+    ctx.check(ctx.L.gca3d_estimate_normals(ctx.h, tgt.h, RADIUS, 0))
+    ctx.check(ctx.L.gca3d_color_gradient(ctx.h, tgt.h, RADIUS))
+    d = tgt.download(normals=True, grad=True)
+    rng = np.random.default_rng(5)
+    xi0 = se3_log(pr.T_gt) + np.concatenate([rng.normal(size=3) * 0.01, rng.normal(size=3) * 0.01])
+    return dict(pr=pr, src=src, tgt=tgt, tn=d["normals"].astype(np.float64), tg=d["grad"].astype(np.float64),
+                xi0=xi0)
+
+
+def _oracle_args(c):
+    pr = c["pr"]
+    return (pr.src_xyz.astype(np.float32).astype(np.float64), pr.src_rgb.astype(np.float32).astype(np.float64),
+            pr.tgt_xyz, pr.tgt_rgb, c["tn"], c["tg"])
+
+
+def _loss_seed(seed):
+    rng = np.random.default_rng(seed)
+    G = rng.normal(size=(4, 4))
+    G[3] = 0.0
+    return G, 0.3
+
+
+@pytest.mark.parametrize("K,umap", [(5, 1), (5, 0), (2, 1)])
+def test_vjp_matches_fp64_adjoint(ctx, N, orc, c2, K, umap):
+    from cuda_3d_gb300 import synth
+
+    G, gE = _loss_seed(K + 10 * umap)
+    r = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], c2["xi0"], K=K, max_corr=MAX_CORR, update_map=umap, dT=G, dE=gE,
+                        want_corr=True)
+    assert r["status"] == N.OK
+    corr = r["corr"]
+    assert (corr >= 0).mean() > 0.3
+    a = _oracle_args(c2)
+    T64, E64, _ = orc.icp_unrolled_f64(*a, c2["xi0"], K=K, max_corr=MAX_CORR, update_map=umap, corr=corr)
+    rot, tr = synth.pose_error(r["T"], T64)
+    assert rot <= POSE_TOL and tr <= POSE_TOL, (rot, tr)
+    assert abs(r["E"] - E64) <= 1e-4 * abs(E64)
+    dxi, dX, dC, st = orc.icp_unrolled_vjp_f64(*a, c2["xi0"], corr, G, gE, K=K, max_corr=MAX_CORR, update_map=umap)
+    assert st == 0
+    for g, ref in ((r["dxyz"], dX), (r["drgb"], dC)):
+        assert np.linalg.norm(g - ref) <= GRAD_RTOL * np.linalg.norm(ref)
+    # the pose gradient: meaningful at K = 2; at K = 5 it has vanished (Gauss-Newton
+    # converged quadratically), so only the absolute level is compared
+    if K <= 2:
+        assert np.linalg.norm(r["dxi0"] - dxi) <= POSE_GRAD_RTOL * np.linalg.norm(dxi)
+    else:
+        assert np.abs(r["dxi0"]).max() <= 1e-3 * np.abs(G).max()
+
+
+def test_vjp_matches_finite_differences(ctx, N, orc, c2):
+    K, umap = 5, 1
+    G, gE = _loss_seed(77)
+    r = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], c2["xi0"], K=K, max_corr=MAX_CORR, update_map=umap, dT=G, dE=gE,
+                        want_corr=True)
+    corr = r["corr"]
+    sx, sc, tx, tc, tn, tg = _oracle_args(c2)
+
+    def L(xi, X, Cc):
+        T, E, _ = orc.icp_unrolled_f64(X, Cc, tx, tc, tn, tg, xi, K=K, max_corr=MAX_CORR, update_map=umap, corr=corr)
+        return (G * T).sum() + gE * E
+
+    rng = np.random.default_rng(3)
+    xi0 = c2["xi0"]
+    # the pose block: K = 5 leaves it at the rounding level on both sides
+    for m in range(6):
+        e = np.zeros(6)
+        e[m] = 1e-4
+        fd = (L(xi0 + e, sx, sc) - L(xi0 - e, sx, sc)) / 2e-4
+        assert abs(r["dxi0"][m] - fd) <= 1e-3 * np.abs(G).max()
+    matched = np.flatnonzero((corr >= 0).all(axis=0))
+    for X, g, h, which in ((sx, r["dxyz"], 1e-5, "xyz"), (sc, r["drgb"], 1e-4, "rgb")):
+        floor = 1e-3 * np.abs(g).max()
+        for i in rng.choice(matched, 29, replace=False):
+            a = int(rng.integers(3))
+            Xp, Xm = X.copy(), X.copy()
+            Xp[i, a] += h
+            Xm[i, a] -= h
+            fd = ((L(xi0, Xp, sc) - L(xi0, Xm, sc)) if which == "xyz" else (L(xi0, sx, Xp) - L(xi0, sx, Xm))) / (2 * h)
+            assert abs(g[i, a] - fd) <= FD_RTOL * max(abs(fd), floor), (which, i, a, g[i, a], fd)
+
+
+def test_vjp_torch_autograd_wrapper(ctx, N, c2):
+    """a thin torch.autograd.Function (test harness only): forward calls the entry
+    point without a cotangent, backward calls it again with one"""
+    import torch
+
+    pr = c2["pr"]
+    dev = torch.device("cuda", 0)
+    K, umap = 5, 1
+    tgt = c2["tgt"]
+    n = len(pr.src_xyz)
+
+    class UnrolledIcp(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, xi0, xyz, rgb):
+            cloud = ctx.cloud(n)
+            torch.cuda.synchronize()
+            ctx.check(ctx.L.gca3d_cloud_upload(ctx.h, cloud.h, xyz.data_ptr(), rgb.data_ptr(), n))
+            r = N.color_icp_vjp(ctx, cloud, tgt, xi0.detach().cpu().numpy(), K=K, max_corr=MAX_CORR,
+                                update_map=umap)
+            fctx.save_for_backward(xi0, xyz, rgb)
+            return torch.tensor(r["T"], dtype=torch.float64), torch.tensor(r["E"], dtype=torch.float64)
+
+        @staticmethod
+        def backward(fctx, gT, gE):
+            xi0, xyz, rgb = fctx.saved_tensors
+            cloud = ctx.cloud(n)
+            torch.cuda.synchronize()
+            ctx.check(ctx.L.gca3d_cloud_upload(ctx.h, cloud.h, xyz.data_ptr(), rgb.data_ptr(), n))
+            dxyz = torch.empty_like(xyz)
+            drgb = torch.empty_like(rgb)
+
+            class Buf:
+                def __init__(self, t):
+                    self.ptr = t.data_ptr()
+
+            r = N.color_icp_vjp(ctx, cloud, tgt, xi0.detach().cpu().numpy(), K=K, max_corr=MAX_CORR,
+                                update_map=umap, dT=gT.detach().cpu().numpy(), dE=float(gE), n_src=n,
+                                out={"dxyz": Buf(dxyz), "drgb": Buf(drgb)})
+            ctx.sync()
+            return torch.tensor(r["dxi0"], dtype=xi0.dtype), dxyz, drgb
+
+    xi0 = torch.tensor(c2["xi0"], dtype=torch.float64, requires_grad=True)
+    xyz = torch.tensor(pr.src_xyz, dtype=torch.float32, device=dev, requires_grad=True)
+    rgb = torch.tensor(pr.src_rgb, dtype=torch.float32, device=dev, requires_grad=True)
+    G, gE = _loss_seed(5)
+    T, E = UnrolledIcp.apply(xi0, xyz, rgb)
+    loss = (torch.tensor(G) * T).sum() + gE * E
+    loss.backward()
+    ref = N.color_icp_vjp(ctx, c2["src"], tgt, c2["xi0"], K=K, max_corr=MAX_CORR, update_map=umap, dT=G, dE=gE)
+    np.testing.assert_array_equal(xyz.grad.cpu().numpy(), ref["dxyz"])
+    np.testing.assert_array_equal(rgb.grad.cpu().numpy(), ref["drgb"])
+    np.testing.assert_array_equal(xi0.grad.numpy(), ref["dxi0"])
+
+
+def test_vjp_rejects_bad_arguments(ctx, N, c2):
+    import ctypes as C
+
+    bad = N.VjpParams(0, MAX_CORR, 0.968, 1)
+    x0 = np.zeros(6)
+    st = ctx.L.gca3d_color_icp_vjp(ctx.h, c2["src"].h, c2["tgt"].h, C.byref(bad), x0.ctypes.data, None, 0.0, None,
+                                   None, None, None, None, None)
+    assert st == N.ERR_INVALID_VALUE
+    # a target without colour gradients
+    plain = ctx.cloud_from(c2["pr"].tgt_xyz, c2["pr"].tgt_rgb)
+    ok = N.VjpParams(5, MAX_CORR, 0.968, 1)
+    st = ctx.L.gca3d_color_icp_vjp(ctx.h, c2["src"].h, plain.h, C.byref(ok), x0.ctypes.data, None, 0.0, None, None,
+                                   None, None, None, None)
+    assert st == N.ERR_INVALID_VALUE
+    # a cotangent without gradient outputs
+    G = np.zeros(16)
+    st = ctx.L.gca3d_color_icp_vjp(ctx.h, c2["src"].h, c2["tgt"].h, C.byref(ok), x0.ctypes.data, G.ctypes.data, 0.0,
+                                   None, None, None, None, None, None)
+    assert st == N.ERR_INVALID_VALUE
