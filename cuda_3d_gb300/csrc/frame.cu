@@ -13,7 +13,7 @@
 // spin) and writes the compacted SoA points directly.  Same arithmetic order as the
 // reference (unfused multiply/add); the filter weights use det_expf below instead
 // of expf, so the CPU oracle reproduces every output bit.
-#include "internal.cuh"
+#include "stages.cuh"
 
 #include <algorithm>
 
@@ -21,20 +21,8 @@ namespace gca3d
 {
 
 constexpr int kFrameThreads = 256;
-constexpr int kMaxFilterRadius = 7;
-constexpr int kMaxFrameWidth = 2048;
 constexpr unsigned long long kRowAgg = 1ull << 62, kRowInc = 2ull << 62, kRowFlag = 3ull << 62;
 
-struct FrameParams
-{
-    int w, h;
-    float fx, fy, cx, cy;     // depth intrinsics
-    float cfx, cfy, ccx, ccy; // colour intrinsics
-    float R[9], t[3];         // depth -> colour, column-major rotation
-    float depth_scale, tmin, tmax;
-    int mode, radius;
-    float sigma_space, sigma_depth;
-};
 
 // exp(x) in FP32: Cody-Waite reduction x = k ln2 + r (ln2 split into a 16-bit head
 // and a tail so k * head is exact), degree-7 Taylor polynomial in Horner form, and
@@ -277,22 +265,21 @@ int frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr
 
 using namespace gca3d;
 
-extern "C" int gca3d_frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr, int w, int h,
-                                    const gca3d_intrinsics *di, const gca3d_intrinsics *ci,
-                                    const gca3d_extrinsics *d2c, float depth_scale, float tmin, float tmax,
-                                    const gca3d_filter *filter, gca3d_cloud *out)
+namespace gca3d
 {
-    // cuda_make_point_cloud (cuda_point_cloud_factory.cu:283-290): parameters present,
-    // depth_scale > 0
-    if (!ctx || !depth || !bgr || !di || !out || w <= 0 || h <= 0)
+// cuda_make_point_cloud (cuda_point_cloud_factory.cu:283-290): parameters present,
+// depth_scale > 0; plus this kernel's limits (width, filter radius)
+int frame_params(gca3d_context *ctx, int w, int h, const gca3d_intrinsics *di, const gca3d_intrinsics *ci,
+                 const gca3d_extrinsics *d2c, float depth_scale, float tmin, float tmax, const gca3d_filter *filter,
+                 FrameParams &P)
+{
+    if (!di || w <= 0 || h <= 0)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "frame_to_cloud: bad arguments");
     if (!(depth_scale > 0.0f))
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "frame_to_cloud: depth_scale must be > 0");
     if (w > kMaxFrameWidth)
         return fail(ctx, GCA3D_ERR_NOT_SUPPORTED, "frame_to_cloud: width above 2048");
-    if ((int64_t)w * h > out->capacity)
-        return fail(ctx, GCA3D_ERR_CAPACITY, "frame_to_cloud: output capacity below w * h");
-    FrameParams P{};
+    P = FrameParams{};
     P.w = w, P.h = h;
     P.fx = di->fx, P.fy = di->fy, P.cx = di->cx, P.cy = di->cy;
     const gca3d_intrinsics *c = ci ? ci : di;
@@ -310,9 +297,25 @@ extern "C" int gca3d_frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, c
                                      (P.radius < 0 || P.radius > kMaxFilterRadius || !(P.sigma_space > 0) ||
                                       !(P.sigma_depth > 0))))
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "frame_to_cloud: bad filter parameters");
-    ctx->arena.reset();
-    int st = frame_to_cloud(ctx, depth, bgr, P, out);
+    return GCA3D_OK;
+}
+} // namespace gca3d
+
+extern "C" int gca3d_frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr, int w, int h,
+                                    const gca3d_intrinsics *di, const gca3d_intrinsics *ci,
+                                    const gca3d_extrinsics *d2c, float depth_scale, float tmin, float tmax,
+                                    const gca3d_filter *filter, gca3d_cloud *out)
+{
+    if (!ctx || !depth || !bgr || !out)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "frame_to_cloud: bad arguments");
+    FrameParams P;
+    int st = frame_params(ctx, w, h, di, ci, d2c, depth_scale, tmin, tmax, filter, P);
     if (st)
+        return st;
+    if ((int64_t)w * h > out->capacity)
+        return fail(ctx, GCA3D_ERR_CAPACITY, "frame_to_cloud: output capacity below w * h");
+    ctx->arena.reset();
+    if ((st = frame_to_cloud(ctx, depth, bgr, P, out)))
         return st;
     out->has_normals = out->has_grad = false;
     return GCA3D_OK;

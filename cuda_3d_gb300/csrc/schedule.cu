@@ -49,6 +49,7 @@ struct gca3d_icp_plan
     int64_t kernels_static = 0; // graph kernels outside the iteration loops
     bool host_checks = false; // plain mode: convergence test read back after every iteration
     cudaStream_t side = nullptr; // captures the bodies of the device-side loops
+    PlanPrologue prologue;       // work enqueued before the schedule (captured with it)
 };
 
 namespace
@@ -228,7 +229,9 @@ int run_with_arena(gca3d_icp_plan *pl, bool capturing)
     pl->ctx->arena.reset();
     const int64_t l0 = pl->ctx->launches;
     pl->kernels_static = 0;
-    int st = run_schedule(pl, capturing);
+    int st = pl->prologue ? pl->prologue(pl->ctx) : GCA3D_OK;
+    if (!st)
+        st = run_schedule(pl, capturing);
     if (!st && pl->ctx->arena.failed)
         st = fail(pl->ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp plan: scratch memory");
     pl->kernels_per_run = pl->ctx->launches - l0;
@@ -291,8 +294,11 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
     return GCA3D_OK;
 }
 
-static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
-                       const gca3d_icp_params *params, bool capture, gca3d_icp_plan **out)
+} // extern "C"
+
+int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
+                                    const gca3d_icp_params *params, bool capture, PlanPrologue prologue,
+                                    gca3d_icp_plan **out)
 {
     if (!ctx || !out || P < 1 || P > kMaxSegments || !src || !tgt)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: bad arguments (1 <= pairs <= 4096)");
@@ -314,6 +320,7 @@ static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d
     pl->tgt.assign(tgt, tgt + P);
     pl->prm = *params;
     pl->host_checks = !params->use_graph;
+    pl->prologue = std::move(prologue);
     int nb = 0;
     for (int k = 0; k < P; ++k)
     {
@@ -406,10 +413,12 @@ static int plan_create(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d
     return GCA3D_OK;
 }
 
+extern "C" {
+
 int gca3d_icp_plan_create(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
                           const gca3d_icp_params *params, gca3d_icp_plan **plan)
 {
-    return plan_create(ctx, n_pairs, src, tgt, params, params && params->use_graph, plan);
+    return icp_plan_create_internal(ctx, n_pairs, src, tgt, params, params && params->use_graph, nullptr, plan);
 }
 
 int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_result *results)
@@ -468,7 +477,7 @@ int gca3d_color_icp_batched(gca3d_context *ctx, int n_pairs, gca3d_cloud *const 
     if (!results)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: results needed");
     gca3d_icp_plan *pl = nullptr;
-    int st = plan_create(ctx, n_pairs, src, tgt, params, false, &pl);
+    int st = icp_plan_create_internal(ctx, n_pairs, src, tgt, params, false, nullptr, &pl);
     if (st)
         return st;
     st = gca3d_icp_plan_execute(pl, T_init, results);

@@ -3,6 +3,8 @@
 
 #include "internal.cuh"
 
+#include <functional>
+
 namespace gca3d
 {
 
@@ -49,6 +51,34 @@ struct Grid
 int seg_bounds(gca3d_context *ctx, const float4 *pos, const int32_t *seg_off, int P, int64_t max_seg_cap,
                int *ord);
 int single_seg_offsets(gca3d_context *ctx, const int32_t *d_n, int32_t *seg_off);
+
+// a depth + colour frame: camera model, filter and limits of the frame kernel
+constexpr int kMaxFilterRadius = 7;
+constexpr int kMaxFrameWidth = 2048;
+struct FrameParams
+{
+    int w, h;
+    float fx, fy, cx, cy;     // depth intrinsics
+    float cfx, cfy, ccx, ccy; // colour intrinsics
+    float R[9], t[3];         // depth -> colour, column-major rotation
+    float depth_scale, tmin, tmax;
+    int mode, radius;
+    float sigma_space, sigma_depth;
+};
+int frame_params(gca3d_context *ctx, int w, int h, const gca3d_intrinsics *di, const gca3d_intrinsics *ci,
+                 const gca3d_extrinsics *d2c, float depth_scale, float tmin, float tmax, const gca3d_filter *filter,
+                 FrameParams &P);
+// filtered, back-projected and compacted frame into `out` (device count); scratch
+// from the context arena; no host synchronisation (capture-safe)
+int frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr, const FrameParams &P,
+                   gca3d_cloud *out);
+
+// an ICP plan whose graph (or eager run) starts with `prologue`, enqueued on the
+// context stream with the plan's arena active (the frame stage of a tracker)
+using PlanPrologue = std::function<int(gca3d_context *)>;
+int icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
+                             const gca3d_icp_params *params, bool capture, PlanPrologue prologue,
+                             gca3d_icp_plan **out);
 
 // a single-segment batch view of a cloud (no copy; segment offsets from the arena)
 int cloud_batch(gca3d_context *ctx, gca3d_cloud *c, Batch &b);

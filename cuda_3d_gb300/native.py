@@ -61,6 +61,12 @@ class IcpResult(C.Structure):
                 ("scale_n_tgt", C.c_int * MAX_SCALES)]
 
 
+class TrackerParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("depth_intrin", Intrinsics), ("color_intrin", Intrinsics),
+                ("depth_to_color", Extrinsics), ("depth_scale", C.c_float), ("tmin", C.c_float), ("tmax", C.c_float),
+                ("filter", Filter), ("icp", IcpParams), ("constant_velocity", C.c_int)]
+
+
 class VjpParams(C.Structure):
     _fields_ = [("K", C.c_int), ("max_corr", C.c_float), ("lambda_", C.c_float), ("update_map", C.c_int)]
 
@@ -111,6 +117,11 @@ _SIGS = {
     "gca3d_icp_plan_execute": [_P, _P, _P],
     "gca3d_icp_plan_destroy": [_P],
     "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
+    "gca3d_tracker_create": [_P, C.POINTER(TrackerParams), C.POINTER(_P)],
+    "gca3d_tracker_destroy": [_P],
+    "gca3d_tracker_frame_buffers": [_P, C.POINTER(_P), C.POINTER(_P)],
+    "gca3d_tracker_push": [_P, _P, _P, C.POINTER(IcpResult), _P],
+    "gca3d_tracker_kernels": [_P, C.POINTER(_I64)],
     "gca3d_color_icp_vjp": [_P, _P, _P, C.POINTER(VjpParams), _P, _P, C.c_double, _P, C.POINTER(C.c_double), _P,
                             _P, _P, _P],
 }
@@ -401,3 +412,60 @@ def color_icp_vjp(ctx, src, tgt, xi0, K=5, max_corr=0.05, lam=0.968, update_map=
     if want_corr:
         res["corr"] = bc.read(np.int32, (K + 1) * n).reshape(K + 1, n)
     return res
+
+
+def tracker_params(cam, scales, depth_scale=0.001, tmin=0.2, tmax=10.0, filter=(FILTER_FIXED, 2, 3.0, 30.0),
+                   constant_velocity=True, **icp_kw):
+    """cam: width, height, fx, fy, cx, cy (identity depth -> colour extrinsic, equal
+    intrinsics); filter: (mode, radius, sigma_space px, sigma_depth in depth units)"""
+    p = TrackerParams()
+    p.width, p.height = cam.width, cam.height
+    p.depth_intrin = Intrinsics(cam.fx, cam.fy, cam.cx, cam.cy)
+    p.color_intrin = Intrinsics(cam.fx, cam.fy, cam.cx, cam.cy)
+    p.depth_to_color = Extrinsics((C.c_float * 9)(1, 0, 0, 0, 1, 0, 0, 0, 1), (C.c_float * 3)(0, 0, 0))
+    p.depth_scale, p.tmin, p.tmax = depth_scale, tmin, tmax
+    p.filter = Filter(*filter)
+    p.icp = icp_params(scales, **icp_kw)
+    p.constant_velocity = int(constant_velocity)
+    return p
+
+
+class Tracker:
+    """frame-to-frame colored-ICP tracking of an RGB-D stream"""
+
+    def __init__(self, ctx, params):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        ctx.check(ctx.L.gca3d_tracker_create(ctx.h, C.byref(params), C.byref(self.h)))
+        self.shape = (params.height, params.width)
+        self._res = IcpResult()
+        self._pose = np.zeros(16, np.float64)
+
+    def frame_buffers(self):
+        """numpy views of the pinned staging (depth H x W uint16, BGR H x W x 3 uint8)"""
+        d, c = C.c_void_p(), C.c_void_p()
+        self.ctx.check(self.ctx.L.gca3d_tracker_frame_buffers(self.h, C.byref(d), C.byref(c)))
+        H, W = self.shape
+        depth = np.ctypeslib.as_array(C.cast(d, C.POINTER(C.c_uint16)), shape=(H, W))
+        bgr = np.ctypeslib.as_array(C.cast(c, C.POINTER(C.c_uint8)), shape=(H, W, 3))
+        return depth, bgr
+
+    def push(self, depth=None, bgr=None):
+        """returns (result dict, camera pose relative to the first frame)"""
+        d = None if depth is None else np.ascontiguousarray(depth, np.uint16)
+        c = None if bgr is None else np.ascontiguousarray(bgr, np.uint8)
+        self.ctx.check(self.ctx.L.gca3d_tracker_push(self.h, _ptr(d), _ptr(c), C.byref(self._res),
+                                                     self._pose.ctypes.data))
+        return result_dict(self._res), self._pose.reshape(4, 4).copy()
+
+    def kernels(self):
+        n = C.c_int64()
+        self.ctx.check(self.ctx.L.gca3d_tracker_kernels(self.h, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.L.gca3d_tracker_destroy(self.h)
+        except Exception:
+            pass

@@ -429,3 +429,82 @@ def spline_poses(n_frames, seed=0, step_m=0.015, step_deg=1.0):
         poses.append(make_T(R, tr))
     p0inv = np.linalg.inv(poses[0])
     return [p0inv @ p for p in poses]
+
+
+# --------------------------------------------------------------------------- #
+# the same frame renderer in torch, for long synthetic sequences on the GPU
+# (data generation only: identical geometry and colour field; the noise comes from
+# a torch generator seeded with the frame seed)
+# --------------------------------------------------------------------------- #
+def _raycast_torch(scene, o, d):
+    import torch
+
+    n = d.shape[0]
+    best = torch.full((n,), math.inf, dtype=d.dtype, device=d.device)
+    sid = torch.full((n,), -1, dtype=torch.int64, device=d.device)
+    k = 0
+
+    def take(t, ok, k, best, sid):
+        return torch.where(ok, t, best), torch.where(ok, torch.full_like(sid, k), sid)
+
+    for nrm, off in scene["planes"]:
+        nv = torch.as_tensor(nrm, dtype=d.dtype, device=d.device)
+        t = (off - o @ nv) / (d @ nv)
+        best, sid = take(t, (t > 1e-6) & (t < best), k, best, sid)
+        k += 1
+    inv = 1.0 / d
+    for lo, hi in scene["boxes"]:
+        lo_t = torch.as_tensor(lo, dtype=d.dtype, device=d.device)
+        hi_t = torch.as_tensor(hi, dtype=d.dtype, device=d.device)
+        t0, t1 = (lo_t - o) * inv, (hi_t - o) * inv
+        a, b = torch.minimum(t0, t1), torch.maximum(t0, t1)
+        tmin = torch.where(torch.isnan(a), -math.inf, a).max(1).values
+        tmax = torch.where(torch.isnan(b), math.inf, b).min(1).values
+        best, sid = take(tmin, (tmax >= tmin) & (tmin > 1e-6) & (tmin < best), k, best, sid)
+        k += 1
+    dd = (d * d).sum(1)
+    for c, r in scene["spheres"]:
+        oc = o - torch.as_tensor(c, dtype=d.dtype, device=d.device)
+        b = (oc * d).sum(1)
+        cc = (oc * oc).sum(1) - r * r
+        disc = b * b - dd * cc
+        t = (-b - torch.sqrt(disc)) / dd
+        best, sid = take(t, (disc >= 0) & (t > 1e-6) & (t < best), k, best, sid)
+        k += 1
+    return best, sid
+
+
+def render_rgbd_torch(scene, T_cam, seed, cam=Camera(), device="cuda", zero_frac=0.05, color_noise=4.0,
+                      depth_noise=True):
+    """render_rgbd on a torch device; returns host numpy depth (H x W uint16) and
+    BGR (H x W x 3 uint8)"""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    f64 = torch.float64
+    u = torch.arange(cam.width, dtype=f64, device=device) - 0.5
+    v = torch.arange(cam.height, dtype=f64, device=device) - 0.5
+    vv, uu = torch.meshgrid(v, u, indexing="ij")
+    dcam = torch.stack([(uu - cam.cx) / cam.fx, (vv - cam.cy) / cam.fy, torch.ones_like(uu)], -1).reshape(-1, 3)
+    T = torch.as_tensor(np.asarray(T_cam), dtype=f64, device=device)
+    dw = dcam @ T[:3, :3].T
+    o = T[:3, 3].expand_as(dw)
+    tt, sid = _raycast_torch(scene, o, dw)
+    hit = o + dw * tt[:, None]
+    z = tt + torch.randn(tt.shape, generator=g, dtype=f64, device=device) * (0.002 * tt * tt) * float(depth_noise)
+    depth = torch.where(torch.isfinite(z) & (z > 0), torch.round(z * 1000.0), torch.zeros_like(z))
+    depth = depth.clamp(0, 65535).to(torch.int32)
+    zero = torch.rand(depth.shape, generator=g, dtype=f64, device=device) < zero_frac
+    depth = torch.where(zero, torch.zeros_like(depth), depth)
+    ok = sid >= 0
+    hp = torch.where(ok[:, None], hit, torch.zeros_like(hit))
+    s = sid.clamp(min=0)
+    colp = torch.as_tensor(scene["colp"], dtype=f64, device=device)[s]
+    colk = torch.as_tensor(scene["colk"], dtype=f64, device=device)[s]
+    col = 128 + 90 * torch.sin((hp[:, None, :] * colk).sum(-1) + colp)
+    col = col + torch.randn(col.shape, generator=g, dtype=f64, device=device) * color_noise
+    col = torch.round(col).clamp(0, 255).to(torch.uint8)
+    bgr = col.flip(1).reshape(cam.height, cam.width, 3)
+    return (depth.reshape(cam.height, cam.width).to(torch.int32).cpu().numpy().astype(np.uint16),
+            bgr.cpu().numpy())

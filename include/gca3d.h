@@ -276,6 +276,39 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *plan);
 int gca3d_icp_plan_kernels(gca3d_icp_plan *plan, int64_t *n);
 
 /* ---------------------------------------------------------------------------
+ * frame-to-frame tracking of an RGB-D stream (the reference's demo loop,
+ * app.cpp:316-350, without its model accumulation)
+ * ------------------------------------------------------------------------- */
+typedef struct gca3d_tracker gca3d_tracker;
+typedef struct gca3d_tracker_params {
+    int width, height;
+    gca3d_intrinsics depth_intrin;
+    gca3d_intrinsics color_intrin;
+    gca3d_extrinsics depth_to_color;
+    float depth_scale, tmin, tmax;
+    gca3d_filter filter;
+    gca3d_icp_params icp;  /* every scale needs voxel > 0; use_graph captures the whole
+                              per-frame sequence as one CUDA graph */
+    int constant_velocity; /* start each registration from the previous relative motion */
+} gca3d_tracker_params;
+
+int gca3d_tracker_create(gca3d_context *ctx, const gca3d_tracker_params *params,
+                         gca3d_tracker **tracker);
+int gca3d_tracker_destroy(gca3d_tracker *tracker);
+/* the pinned host staging of the next frame (depth uint16[w*h], colour BGR
+ * uint8[w*h*3]); a producer may write there and push with NULL frame pointers */
+int gca3d_tracker_frame_buffers(gca3d_tracker *tracker, uint16_t **depth, uint8_t **bgr);
+/* process one frame (host pointers, copied into the staging, or NULL).  For every
+ * frame after the first, result (may be NULL) is the registration of the new frame
+ * onto the previous one: T maps the new camera's coordinates into the previous
+ * camera's.  pose (may be NULL): the camera pose relative to the first frame
+ * (row-major 4x4).  The first frame's result has status GCA3D_ERR_NO_CORRESPONDENCES. */
+int gca3d_tracker_push(gca3d_tracker *tracker, const uint16_t *depth, const uint8_t *bgr,
+                       gca3d_icp_result *result, double pose[16]);
+/* kernels the last push launched */
+int gca3d_tracker_kernels(gca3d_tracker *tracker, int64_t *n);
+
+/* ---------------------------------------------------------------------------
  * adjoint of K unrolled Gauss-Newton steps (no reference counterpart)
  * ------------------------------------------------------------------------- */
 #define GCA3D_VJP_MAX_STEPS 64
