@@ -117,6 +117,9 @@ _SIGS = {
     "gca3d_icp_plan_execute": [_P, _P, _P],
     "gca3d_icp_plan_destroy": [_P],
     "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
+    "gca3d_radius_outlier_removal": [_P, _P, _F, C.c_int, _P],
+    "gca3d_cloud_select": [_P, _P, _P, _I64, _P],
+    "gca3d_cloud_to_aos": [_P, _P, _P, _P],
     "gca3d_tracker_create": [_P, C.POINTER(TrackerParams), C.POINTER(_P)],
     "gca3d_tracker_destroy": [_P],
     "gca3d_tracker_frame_buffers": [_P, C.POINTER(_P), C.POINTER(_P)],

@@ -196,6 +196,24 @@ int gca3d_estimate_normals(gca3d_context *ctx, gca3d_cloud *cloud, float radius,
  * (src/registration/cuda_compute_color_gradient.cu:92-127); needs normals */
 int gca3d_color_gradient(gca3d_context *ctx, gca3d_cloud *cloud, float radius);
 
+/* points with more than min_neighbors neighbours (the point itself included) within
+ * radius, in input order, without normals.  out->capacity >= in->capacity.
+ * reference: point_cloud::radius_outlier_removal (src/geometry/point_cloud.cu:238-280),
+ * cuda_grid_radius_outliers_removal (src/geometry/cuda_nn_search.cu:416-542,725-800) */
+int gca3d_radius_outlier_removal(gca3d_context *ctx, gca3d_cloud *in, float radius,
+                                 int min_neighbors, gca3d_cloud *out);
+
+/* out[k] = in[idx[k]] for k < n (points, colours and normals when present); idx is
+ * host or device memory; an index outside the cloud gives GCA3D_ERR_INVALID_VALUE.
+ * reference: point_cloud::create_new_by_index (src/geometry/point_cloud.cu:438-453) */
+int gca3d_cloud_select(gca3d_context *ctx, gca3d_cloud *in, const int32_t *idx, int64_t n,
+                       gca3d_cloud *out);
+
+/* the cloud as the reference's 28-byte point_t records (geometry/type.hpp:65-70,
+ * property = active) into device memory, and the normals as float3 (may be NULL).
+ * Stream-ordered; no synchronisation. */
+int gca3d_cloud_to_aos(gca3d_context *ctx, gca3d_cloud *cloud, void *d_points, float *d_normals);
+
 /* nearest reference point within radius for every query point, -1 if none; ties on
  * distance go to the smaller index.  out_idx: device int32[n_query].
  * reference: point_cloud::nn_search (src/geometry/point_cloud.cu:506-557),

@@ -1,0 +1,5 @@
+// cuda_container/cuda_container.hpp -- include path of the reference header of the same name; the
+// definitions are in gca_compat_cloud.hpp.
+#pragma once
+
+#include "../gca_compat_cloud.hpp"

@@ -1,0 +1,5 @@
+// registration/color_icp.hpp -- include path of the reference header of the same name; the
+// definitions are in gca_compat_icp.hpp.
+#pragma once
+
+#include "../gca_compat_icp.hpp"

@@ -1871,3 +1871,62 @@ int orc_icp_unrolled_vjp_f64(const double *sx, const double *srgb, int64_t ns, c
     unroll_close(&u);
     return status;
 }
+
+/* ------------------------------------------------------------------ */
+/* radius outlier removal (point_cloud.cu:238-280,                     */
+/* cuda_nn_search.cu:416-542,725-800): cell 2r, origin min - 1.5 cells; */
+/* per axis the own cell and the nearer neighbour (lower corner fused   */
+/* cell * c + origin); count d^2 < r^2 with d = q - p, self included;   */
+/* keep when the count exceeds min_nn; survivors in input order.        */
+/* ------------------------------------------------------------------ */
+int64_t orc_radius_outlier_removal(const float *xyz, const float *rgb, int64_t n, float radius, int min_nn,
+                                   float *out_xyz, float *out_rgb)
+{
+    if (n <= 0)
+        return 0;
+    float mn[3], mx[3], gmin[3];
+    orc_aabb(xyz, n, 1, mn, mx);
+    const float cell = 2.0f * radius, pad = 1.5f * cell, rr = radius * radius;
+    for (int a = 0; a < 3; ++a)
+        gmin[a] = mn[a] - pad;
+    ogrid g;
+    grid_build(&g, xyz, n, gmin, cell);
+    int64_t m = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        f3 p = f3load(xyz, i);
+        float pv[3] = {p.x, p.y, p.z};
+        int32_t c[3];
+        int b[3], e[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = floor_div_key(pv[a], gmin[a], cell);
+            float lo = fmaf(cell, (float)c[a], gmin[a]);
+            float off = pv[a] - lo;
+            b[a] = off >= radius ? 0 : -1;
+            e[a] = off < radius ? 1 : 2;
+        }
+        int count = 0;
+        for (int dx = b[0]; dx < e[0]; ++dx)
+            for (int dy = b[1]; dy < e[1]; ++dy)
+                for (int dz = b[2]; dz < e[2]; ++dz) {
+                    int32_t x = c[0] + dx, y = c[1] + dy, z = c[2] + dz;
+                    for (int64_t s = grid_lower(&g, x, y, z); s < g.n; ++s) {
+                        const vkey *k = &g.cells[s];
+                        if (k->k[0] != x || k->k[1] != y || k->k[2] != z)
+                            break;
+                        f3 q = f3load(xyz, k->idx);
+                        float ddx = q.x - p.x, ddy = q.y - p.y, ddz = q.z - p.z;
+                        float d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        count += d2 < rr;
+                    }
+                }
+        if (count > min_nn) {
+            for (int a = 0; a < 3; ++a) {
+                out_xyz[3 * m + a] = xyz[3 * i + a];
+                out_rgb[3 * m + a] = rgb[3 * i + a];
+            }
+            ++m;
+        }
+    }
+    grid_free(&g);
+    return m;
+}

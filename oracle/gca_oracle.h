@@ -89,6 +89,12 @@ void orc_normals_ref32(const float *xyz, int64_t n, float radius, const float gr
  * max_nn > 0 keeps the max_nn nearest (distance, index) neighbours. */
 void orc_normals_f64(const float *xyz, int64_t n, float radius, int max_nn, double *out_nrm);
 
+/* radius outlier removal (geometry/point_cloud.cu:238-280, cuda_nn_search.cu:416-542,
+ * 725-800): survivors (more than min_nn neighbours within radius, self included) in
+ * input order; returns their count */
+int64_t orc_radius_outlier_removal(const float *xyz, const float *rgb, int64_t n, float radius, int min_nn,
+                                   float *out_xyz, float *out_rgb);
+
 /* colour gradient (registration/cuda_compute_color_gradient.cu:13-127,
  * util/little_3x3_ldlt_solve.cuh) */
 void orc_gradient_ref32(const float *xyz, const float *rgb, const float *nrm, int64_t n,

@@ -97,6 +97,7 @@ def _bind(L):
         "orc_color_icp_ref32": (v, [F32, F32, i64, F32, F32, F32, F32, i64, C.c_int, C.c_float,
                                     F32, C.POINTER(IcpResult)]),
         "orc_pose_jacobian": (v, [F64, C.c_int, F64]),
+        "orc_radius_outlier_removal": (i64, [F32, F32, i64, C.c_float, C.c_int, F32, F32]),
         "orc_icp_unrolled_f64": (C.c_double, [F64, F64, i64, F32, F32, F64, F64, i64,
                                               C.POINTER(UnrollParams), F64, C.c_void_p, C.c_void_p, F64]),
         "orc_icp_unrolled_vjp_f64": (C.c_int, [F64, F64, i64, F32, F32, F64, F64, i64,
@@ -201,6 +202,13 @@ def radius_search(q, r, radius, grid_min):
     lst = np.zeros(max(total, 1), np.int32)
     lib().orc_radius_search(q, len(q), r, len(r), radius, gm, counts, starts, lst.ctypes.data, total)
     return counts, starts, lst[:total]
+
+
+def radius_outlier_removal(xyz, rgb, radius, min_nn):
+    xyz, rgb = _f32(xyz), _f32(rgb)
+    ox, oc = np.zeros_like(xyz), np.zeros_like(rgb)
+    m = lib().orc_radius_outlier_removal(xyz, rgb, len(xyz), float(radius), int(min_nn), ox, oc)
+    return ox[:m], oc[:m]
 
 
 def normals_ref32(xyz, radius, grid_min=None):

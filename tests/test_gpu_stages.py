@@ -335,3 +335,61 @@ def test_frame_tmin_zero_nan_quirk(ctx, N, orc, frames):
     ox, _ = orc.make_point_cloud(frames.depth0, frames.bgr0, (525.0, 525.0, 319.5, 239.5), mode=1, tmin=0.0)
     assert np.isnan(ox).any()
     np.testing.assert_array_equal(d["xyz"], ox)
+
+
+# --------------------------------------------------------------------------- #
+# radius outlier removal, gather by index, AoS view
+# --------------------------------------------------------------------------- #
+def _ror(ctx, xyz, rgb, radius, min_nn):
+    c = ctx.cloud_from(xyz, rgb)
+    out = ctx.cloud(len(xyz))
+    ctx.check(ctx.L.gca3d_radius_outlier_removal(ctx.h, c.h, radius, min_nn, out.h))
+    return out.download()
+
+
+def test_radius_outlier_removal_golden(ctx, golden):
+    xyz, rgb = golden["cloud_xyz"][:8000], golden["cloud_rgb"][:8000]
+    d = _ror(ctx, xyz, rgb, float(golden["ror_radius"]), int(golden["ror_min_nn"]))
+    np.testing.assert_array_equal(d["xyz"], golden["ror_xyz"])
+    np.testing.assert_array_equal(d["rgb"], golden["ror_rgb"])
+
+
+@pytest.mark.parametrize("radius,min_nn", [(0.01, 2), (0.02, 8), (0.05, 40)])
+def test_radius_outlier_removal_full_size_vs_oracle(ctx, orc, room, radius, min_nn):
+    xyz, rgb = room
+    d = _ror(ctx, xyz, rgb, radius, min_nn)
+    ox, oc = orc.radius_outlier_removal(xyz, rgb, radius, min_nn)
+    assert 0 < len(ox) < len(xyz)
+    np.testing.assert_array_equal(d["xyz"], ox)
+    np.testing.assert_array_equal(d["rgb"], oc)
+
+
+def test_radius_outlier_removal_invalid(ctx, N, golden):
+    c = ctx.cloud_from(golden["cloud_xyz"][:100], golden["cloud_rgb"][:100])
+    small = ctx.cloud(10)
+    assert ctx.L.gca3d_radius_outlier_removal(ctx.h, c.h, 0.0, 2, c.h) == N.ERR_INVALID_VALUE
+    assert ctx.L.gca3d_radius_outlier_removal(ctx.h, c.h, 0.05, 2, small.h) == N.ERR_CAPACITY
+
+
+def test_cloud_select_and_aos(ctx, N, golden):
+    xyz, rgb = golden["cloud_xyz"][:5000], golden["cloud_rgb"][:5000]
+    c = ctx.cloud_from(xyz, rgb)
+    c.set_normals(golden["normals"][:5000] if len(golden["normals"]) >= 5000 else np.tile([0, 0, 1.0], (5000, 1)))
+    idx = np.random.default_rng(0).integers(0, 5000, 777).astype(np.int32)
+    out = ctx.cloud(1000)
+    ctx.check(ctx.L.gca3d_cloud_select(ctx.h, c.h, idx.ctypes.data, len(idx), out.h))
+    d = out.download(normals=True)
+    np.testing.assert_array_equal(d["xyz"], xyz[idx])
+    np.testing.assert_array_equal(d["rgb"], rgb[idx])
+    # an index outside the cloud is reported
+    bad = np.array([0, 5000], np.int32)
+    assert ctx.L.gca3d_cloud_select(ctx.h, c.h, bad.ctypes.data, 2, out.h) == N.ERR_INVALID_VALUE
+    # the 28-byte records of the reference's point_t
+    buf = ctx.alloc(28 * 5000)
+    nb = ctx.alloc(12 * 5000)
+    ctx.check(ctx.L.gca3d_cloud_to_aos(ctx.h, c.h, buf.ptr, nb.ptr))
+    raw = buf.read(np.uint8, 28 * 5000).reshape(5000, 28)
+    f = raw[:, :24].copy().view(np.float32).reshape(5000, 6)
+    np.testing.assert_array_equal(f[:, :3], xyz)
+    np.testing.assert_array_equal(f[:, 3:], rgb)
+    assert np.all(raw[:, 24] == 1)

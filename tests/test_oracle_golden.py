@@ -134,3 +134,12 @@ def test_filter_exp_error_bound(orc):
     sub = t <= np.finfo(np.float32).tiny
     assert np.all(np.abs(y[sub] - t[sub]) <= np.finfo(np.float32).smallest_subnormal)
     assert orc.exp32([np.float32(100.0)])[0] == np.inf and orc.exp32([np.float32(-200.0)])[0] == 0.0
+
+
+def test_radius_outlier_removal(golden, orc):
+    """survivors and their order, bit for bit (reference: cuda_nn_search.cu:416-542,725-800)"""
+    xyz, rgb = golden["cloud_xyz"][:8000], golden["cloud_rgb"][:8000]
+    ox, oc = orc.radius_outlier_removal(xyz, rgb, golden["ror_radius"], int(golden["ror_min_nn"]))
+    assert 0 < len(ox) < len(xyz)
+    np.testing.assert_array_equal(ox, golden["ror_xyz"])
+    np.testing.assert_array_equal(oc, golden["ror_rgb"])
