@@ -13,6 +13,11 @@ A step registers the whole batch.  Metric: pairs/s (higher is better).
          uploaded from pinned memory and the 64 results read back
   plain  the one-pair-per-launch FP32 path: 64 sequential single-pair calls, eager
          launches, convergence read back on the host after every iteration
+  rows   the other workloads, each chosen vs plain where both exist: a 640x480
+         frame pair end to end (ms/frame), one 250k-point pair through three
+         scales, the adjoint of 5 unrolled Gauss-Newton steps on a 100k-point pair,
+         and a tracked RGB-D stream at 640x480 and 1280x720 (frames/s, p50/p99
+         latency, drift against the ground-truth trajectory)
 
 --impl reference times the reference's algorithm on the host cores (the CPU port
 in oracle/, FP32 in the reference's operation order, OpenMP) on the same workload.
@@ -55,6 +60,12 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--quick", action="store_true", help="value only (for profiler runs)")
+    p.add_argument("--eager", action="store_true", help="with --quick: the chosen configuration launched "
+                   "eagerly with host convergence checks (the same kernels and iteration counts as the graph; "
+                   "for profilers that do not descend into conditional graph nodes)")
+    p.add_argument("--no-extras", action="store_true", help="skip the per-row measurements (frame pair, "
+                   "single pair, adjoint, stream)")
+    p.add_argument("--stream-frames", type=int, default=200, help="frames of the 640x480 stream (720p: half)")
     return p.parse_args(argv)
 
 
@@ -235,7 +246,8 @@ def run_ours(args):
     srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
     tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
     scales = [N.scale(*s) for s in SCALES]
-    chosen = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True, use_graph=True)
+    chosen = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True,
+                          use_graph=not (args.quick and args.eager))
     plan = N.IcpPlan(ctx, srcs, tgts, chosen)
     res_chosen = None
     for _ in range(max(args.warmup, 3)):
@@ -316,7 +328,8 @@ def run_ours(args):
         plan_prof.execute(results=True)
         t, n = ctx.profile_read()
         breakdown[k] = {"ms": t, "launches": n}
-    roofline = {"kernel": "k_icp_iter (fused NN + residual + Jacobian + JTJ/JTr + FP64 solve)", "bound": "hbm",
+    roofline = {"kernel": "ICP iteration (k_icp_nn + k_icp_accum: transform, NN, residuals, Jacobians, "
+                          "compensated JTJ/JTr, FP64 solve)", "bound": "hbm",
                 "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
@@ -341,6 +354,9 @@ def run_ours(args):
                  "max_pose_diff_vs_chosen": {"rad": rot, "m": tr}}
 
     gt = [synth.pose_error(r["T"], p.T_gt) for r, p in zip(res_chosen, pairs)]
+    rows = None
+    if rank == 0 and not args.no_extras:
+        rows = run_rows(ctx, N, synth, args)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(pairs, sample=4)
@@ -360,6 +376,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "plain": plain,
         "kernel_breakdown_ms_per_execute": breakdown,
+        "rows": rows,
         "gt_error_max": {"rad": max(g[0] for g in gt), "m": max(g[1] for g in gt)},
         "gt_error_median": {"rad": statistics.median(g[0] for g in gt), "m": statistics.median(g[1] for g in gt)},
         "clocks": clk,
@@ -367,6 +384,113 @@ def run_ours(args):
     }
     if rank == 0:
         print(json.dumps(line))
+
+
+# --------------------------------------------------------------------------- #
+# the other workloads
+# --------------------------------------------------------------------------- #
+C0_SCALE = (0.01, 30, 0.03, 0.02, 0.02, 30)  # voxel, iterations, max_corr, normal r, gradient r, max_nn
+
+
+def _lat(ms):
+    ms = np.asarray(ms)
+    return {"p50_ms": float(np.median(ms)), "p99_ms": float(np.percentile(ms, 99)), "mean_ms": float(ms.mean())}
+
+
+def _track(N, ctx, cam, frames, use_graph, compensated, constant_velocity=True):
+    tr = N.Tracker(ctx, N.tracker_params(cam, [N.scale(*C0_SCALE)], use_graph=use_graph, compensated=compensated,
+                                         constant_velocity=constant_velocity))
+    lat, res, pose = [], [], None
+    for d, c in frames:
+        t0 = time.perf_counter()
+        r, pose = tr.push(d, c)
+        lat.append((time.perf_counter() - t0) * 1e3)
+        res.append(r)
+    return lat, res, pose, tr.kernels()
+
+
+def run_rows(ctx, N, synth, args):
+    """per-row measurements on rank 0 (host-timed around calls that return results)"""
+    rows = {}
+    # C0: a 640x480 frame pair end to end (upload, filter, cloud, voxel, normals,
+    # ICP, pose read-back).  The two views alternate through one tracker, so every
+    # push registers one frame pair; the first pushes build the two slot graphs and
+    # are left out.
+    fp = synth.frame_pair(seed=0)
+    cam = fp.cam
+    seq = [(fp.depth0, fp.bgr0), (fp.depth1, fp.bgr1)] * 10
+    out = {}
+    for name, g, comp in (("chosen", True, True), ("plain", False, False)):
+        lat, res, pose, kern = _track(N, ctx, cam, seq, g, comp, constant_velocity=False)
+        rot, tr = synth.pose_error(res[1]["T"], fp.T_gt)
+        out[name] = dict(_lat(lat[4:]), iterations=res[1]["iterations"], n_src=res[1]["n_src"],
+                         gt_error={"rad": rot, "m": tr}, kernels=kern, T=res[1]["T"])
+    rot, tr = synth.pose_error(out["chosen"].pop("T"), out["plain"].pop("T"))
+    rows["frame_pair_640x480"] = {"unit": "ms/frame pair (host buffers in, pose out; steady state)",
+                                  **out, "chosen_vs_plain_pose_diff": {"rad": rot, "m": tr},
+                                  "plain_over_chosen_ms": out["plain"]["p50_ms"] / out["chosen"]["p50_ms"]}
+
+    # C1: one 250k-point pair, three scales
+    pr = synth.room_pair(seed=1, n_points=250_000, rot_deg=10.0, trans=0.10)
+    s = ctx.cloud_from(pr.src_xyz, pr.src_rgb)
+    t = ctx.cloud_from(pr.tgt_xyz, pr.tgt_rgb)
+    scales = [N.scale(*x) for x in SCALES]
+    one = {}
+    for name, g, comp in (("chosen", True, True), ("plain", False, False)):
+        plan = N.IcpPlan(ctx, [s], [t], N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=comp,
+                                                      use_graph=g))
+        ms = []
+        for k in range(8):
+            t0 = time.perf_counter()
+            r = plan.execute(results=True)[0]
+            ms.append((time.perf_counter() - t0) * 1e3)
+        rot, tr = synth.pose_error(r["T"], pr.T_gt)
+        one[name] = dict(_lat(ms[2:]), iterations=r["iterations"], gt_error={"rad": rot, "m": tr})
+    rows["single_pair_250k_three_scale"] = {"unit": "ms/pair", **one,
+                                            "plain_over_chosen_ms": one["plain"]["p50_ms"] / one["chosen"]["p50_ms"]}
+
+    # C2: adjoint of 5 unrolled Gauss-Newton steps, 100k-point pair
+    pr = synth.room_pair(seed=21, n_points=100_000, rot_deg=10.0, trans=0.10)
+    s = ctx.cloud_from(pr.src_xyz, pr.src_rgb)
+    t = ctx.cloud_from(pr.tgt_xyz, pr.tgt_rgb)
+    ctx.check(ctx.L.gca3d_estimate_normals(ctx.h, t.h, 0.06, 0))
+    ctx.check(ctx.L.gca3d_color_gradient(ctx.h, t.h, 0.06))
+    G = np.random.default_rng(1).normal(size=(4, 4))
+    G[3] = 0
+    xi0 = np.zeros(6)
+    bufs = {"dxyz": ctx.alloc(12 * 100_000), "drgb": ctx.alloc(12 * 100_000)}
+    fwd, bwd = [], []
+    for k in range(12):
+        t0 = time.perf_counter()
+        N.color_icp_vjp(ctx, s, t, xi0, K=5, max_corr=0.05, n_src=100_000)
+        t1 = time.perf_counter()
+        N.color_icp_vjp(ctx, s, t, xi0, K=5, max_corr=0.05, dT=G, dE=0.3, n_src=100_000, out=bufs)
+        t2 = time.perf_counter()
+        fwd.append((t1 - t0) * 1e3)
+        bwd.append((t2 - t1) * 1e3)
+    rows["adjoint_100k_K5"] = {"unit": "ms per call", "forward_only": _lat(fwd[2:]),
+                               "forward_and_gradient": _lat(bwd[2:]),
+                               "note": "gradient accuracy is tested against FP64 central differences and the "
+                                       "FP64 adjoint (tests/test_gpu_vjp.py)"}
+
+    # C4: tracked stream, 640x480 and 1280x720
+    scene = synth.frame_scene(1234)
+    for name, cam, nf in (("640x480", synth.Camera(), args.stream_frames),
+                          ("1280x720", synth.Camera(1280, 720, 1050.0, 1050.0, 639.5, 359.5),
+                           max(args.stream_frames // 2, 4))):
+        poses = synth.spline_poses(nf, seed=0)
+        frames = [synth.render_rgbd_torch(scene, P, 1000 + k, cam) for k, P in enumerate(poses)]
+        row = {"frames": nf}
+        for arm, g, comp in (("chosen", True, True), ("plain", False, False)):
+            lat, res, pose, kern = _track(N, ctx, cam, frames, g, comp)
+            lat = lat[3:]
+            rot, tr = synth.pose_error(pose, poses[-1])
+            row[arm] = dict(_lat(lat), frames_per_s=1e3 / float(np.mean(lat)),
+                            drift={"rad": rot, "m": tr, "per_frame_m": tr / (nf - 1)},
+                            mean_iterations=float(np.mean([r["iterations"] for r in res[1:]])),
+                            mean_src_points=float(np.mean([r["n_src"] for r in res[1:]])), kernels_per_frame=kern)
+        rows[f"stream_{name}"] = row
+    return rows
 
 
 # --------------------------------------------------------------------------- #

@@ -29,7 +29,10 @@
 namespace gca3d
 {
 
-// accumulator of kTerms values: plain FP32 or FP32 value + FP32 error (two-sum)
+// accumulator of kTerms values.  A thread sums its own few points (kIcpChunk /
+// kIcpThreads = 4) in plain FP32; with Comp every combination above that -- the
+// shuffle tree, the cross-warp sum -- is an error-free two-sum carrying an FP32
+// error term, so the block sum is compensated where its error would grow.
 template <bool Comp> struct Acc
 {
     float s[kTerms];
@@ -40,18 +43,7 @@ template <bool Comp> struct Acc
         for (int k = 0; k < kTerms; ++k)
             s[k] = 0.0f, e[k] = 0.0f;
     }
-    __device__ __forceinline__ void add(int k, float x)
-    {
-        if (Comp)
-        {
-            const float t = s[k] + x;
-            const float bp = t - s[k];
-            e[k] += (s[k] - (t - bp)) + (x - bp);
-            s[k] = t;
-        }
-        else
-            s[k] += x;
-    }
+    __device__ __forceinline__ void add(int k, float x) { s[k] += x; }
     __device__ __forceinline__ void add_terms(const GNTerms &o, float d2)
     {
         int u = 0;
@@ -184,6 +176,7 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
                 S.scale_iters[k] = S.scale_nsrc[k] = S.scale_ntgt[k] = 0;
         }
         S.scale = scale;
+        S.nn_warm = 0;
         S.scale_nsrc[scale] = ns;
         S.scale_ntgt[scale] = nt;
         if (nb == 0)
@@ -239,10 +232,14 @@ __device__ __forceinline__ BlockPair block_pair(const int32_t *src_off, const Pa
 }
 
 // step 1 of an iteration: the correspondence of every active source point
-// (grid position and squared distance, -1 when none within max_corr)
+// (grid position and squared distance, -1 when none within max_corr).  From the
+// second iteration of a scale on, the point's previous correspondence (same grid)
+// is a candidate at a known distance u: the search shrinks to the cells that
+// overlap the ball of radius u, which holds the nearest point and all its ties.
 __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                         GridDev g, const PairState *st, const int *bmap, int P,
-                                                        float max_corr, int2 *corr, int32_t *nn_out)
+                                                        float max_corr, int2 *corr, const int2 *corr_prev,
+                                                        int32_t *nn_out)
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
@@ -253,13 +250,27 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
     const float3 o = g.gmin[b.pair];
     const float rr = __fmul_rn(max_corr, max_corr);
     const int tbase = g.seg_off[b.pair];
+    const bool warm = corr_prev && st[b.pair].nn_warm;
     // four lanes per source point (uniform trip count for the whole block)
     for (int base = b.start; base < b.end; base += kIcpThreads / kSub)
     {
         const int i = base + (int)(threadIdx.x / kSub);
         const bool valid = i < b.end;
         const float3 p = apply_pose(s_T, src_pos[valid ? i : b.start]);
-        const NNBest best = nn_search_sub(g, L, b.pair, o, p, rr, valid);
+        CellBox B;
+        const bool in = nn_full_box(g, L, o, p, B);
+        if (warm && valid && in)
+        {
+            const int t = corr_prev[i].x;
+            if (t >= 0)
+            {
+                const float4 q = __ldg(&g.spos[t]);
+                const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+                if (d2 < rr)
+                    nn_shrink_box(g, o, p, sqrtf(d2), B);
+            }
+        }
+        const NNBest best = nn_search_box(g, L, b.pair, B, p, rr, valid && in);
         if (valid && (threadIdx.x & (kSub - 1)) == 0)
         {
             corr[i] = make_int2(best.t, __float_as_int(best.d2));
@@ -269,24 +280,21 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
     }
 }
 
-// step 2: residuals, Jacobians, compensated block sums; the pair's last block
-// solves and updates the pose
+// step 2: residuals, Jacobians, block sums (one partial per block)
 template <bool Comp>
 __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                            const float4 *__restrict__ tpos,
                                                            const float4 *__restrict__ attr0,
                                                            const float4 *__restrict__ attr1,
-                                                           const int2 *__restrict__ corr, PairState *st,
-                                                           const int *bmap, int P, double *partials, IcpScale prm)
+                                                           const int2 *__restrict__ corr, const PairState *st,
+                                                           const int *bmap, int P, double *partials, float slg,
+                                                           float slc)
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
-    __shared__ int s_last;
     const BlockPair b = block_pair(src_off, st, bmap, P, kIcpChunk, s_T, &s_pair);
-    const int pair = b.pair;
-    if (pair < 0)
+    if (b.pair < 0)
         return;
-    const int bstart = bmap[pair];
     Acc<Comp> acc;
     acc.zero();
     for (int i = b.start + threadIdx.x; i < b.end; i += kIcpThreads)
@@ -301,129 +309,128 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restr
         const float4 a1 = __ldg(&attr1[c.x]);
         GNTerms terms;
         gn_terms(p, s4.w, make_float3(q.x, q.y, q.z), a0.w, make_float3(a0.x, a0.y, a0.z),
-                 make_float3(a1.x, a1.y, a1.z), prm.sqrt_lg, prm.sqrt_lc, terms);
+                 make_float3(a1.x, a1.y, a1.z), slg, slc, terms);
         acc.add_terms(terms, __int_as_float(c.y));
     }
     block_reduce_store<Comp>(acc, partials + (size_t)blockIdx.x * kTermsPad);
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        const unsigned t = atomicAdd(&st[pair].ticket, 1u);
-        s_last = (int)t == st[pair].nblocks - 1;
-    }
-    __syncthreads();
-    if (!s_last)
-        return;
-    // ---- last block of the pair: reduce the partials in block order --------
+}
+
+// step 3, one block per pair: the pair's block partials summed in FP64 in block
+// order, the 6x6 solve, the step map, the FP64 pose update and the reference's
+// convergence test (color_icp.cu:216-228).  With a loop, the last block to finish
+// decides whether the device-side iteration loop goes on: while a pair is active
+// and the scale's budget lasts.
+template <bool Comp>
+__global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int P, const int *bmap,
+                                                              const double *partials, IcpScale prm, IcpLoop loop)
+{
+    const int pair = blockIdx.x;
+    PairState &Ps = st[pair];
     __shared__ double s_red[kIcpThreads / 32][kTermsPad];
-    const int nb = st[pair].nblocks;
-    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
-    if (lane < kTerms)
+    __shared__ int s_last;
+    if (Ps.active)
     {
-        double v = 0.0;
-        float vf = 0.0f;
-        for (int j = grp; j < nb; j += kIcpThreads / 32)
-        {
-            const double x = __ldcg(partials + (size_t)(bstart + j) * kTermsPad + lane);
-            if (Comp)
-                v += x;
-            else
-                vf += (float)x;
-        }
-        s_red[grp][lane] = Comp ? v : (double)vf;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-        double S[kTerms];
-        for (int k = 0; k < kTerms; ++k)
+        const int nb = Ps.nblocks, bstart = bmap[pair];
+        const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+        if (lane < kTerms)
         {
             double v = 0.0;
             float vf = 0.0f;
-            for (int w = 0; w < kIcpThreads / 32; ++w)
+            for (int j = grp; j < nb; j += kIcpThreads / 32)
             {
+                const double x = partials[(size_t)(bstart + j) * kTermsPad + lane];
                 if (Comp)
-                    v += s_red[w][k];
+                    v += x;
                 else
-                    vf += (float)s_red[w][k];
+                    vf += (float)x;
             }
-            S[k] = Comp ? v : (double)vf;
+            s_red[grp][lane] = Comp ? v : (double)vf;
         }
-        PairState &Ps = st[pair];
-        const double ns = (double)Ps.nsrc;
-        Ps.rmse_ref = S[27] / ns;
-        Ps.fitness = S[28] / ns;
-        Ps.inlier_rmse = S[28] > 0.0 ? sqrt(S[29] / S[28]) : 0.0;
-        double x[6], Ti[16];
-        const int singular = solve6_device(S, x);
-        if (prm.trace && Ps.iters < prm.trace_cap)
+        __syncthreads();
+        if (threadIdx.x == 0)
         {
-            IcpTrace &tr = prm.trace[(size_t)Ps.iters * P + pair];
-            for (int k = 0; k < 16; ++k)
-                tr.T[k] = Ps.T[k];
+            double S[kTerms];
             for (int k = 0; k < kTerms; ++k)
-                tr.S[k] = S[k];
-            for (int k = 0; k < 6; ++k)
-                tr.x[k] = x[k];
-            tr.status = singular;
-        }
-        if (S[28] == 0.0)
-            Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
-        else if (singular && Ps.status == 0)
-            Ps.status = GCA3D_ERR_SINGULAR;
-        pose_from_x_device(x, prm.update_map, Ti);
-        double Tn[16];
-        for (int r = 0; r < 4; ++r)
-            for (int c = 0; c < 4; ++c)
             {
                 double v = 0.0;
-                for (int k = 0; k < 4; ++k)
-                    v += Ti[4 * r + k] * Ps.T[4 * k + c];
-                Tn[4 * r + c] = v;
+                float vf = 0.0f;
+                for (int w = 0; w < kIcpThreads / 32; ++w)
+                {
+                    if (Comp)
+                        v += s_red[w][k];
+                    else
+                        vf += (float)s_red[w][k];
+                }
+                S[k] = Comp ? v : (double)vf;
             }
-        for (int k = 0; k < 16; ++k)
-            Ps.T[k] = Tn[k];
-        Ps.iters += 1;
-        Ps.scale_iters[Ps.scale] += 1;
-        // convergence test of color_icp.cu:216-228 on this step
-        const double cth = 0.5 * (Ti[0] + Ti[5] + Ti[10] - 1.0);
-        const double tsq = Ti[3] * Ti[3] + Ti[7] * Ti[7] + Ti[11] * Ti[11];
-        if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
-        {
-            Ps.converged = 1;
-            Ps.active = 0;
+            const double ns = (double)Ps.nsrc;
+            Ps.rmse_ref = S[27] / ns;
+            Ps.fitness = S[28] / ns;
+            Ps.inlier_rmse = S[28] > 0.0 ? sqrt(S[29] / S[28]) : 0.0;
+            double x[6], Ti[16];
+            const int singular = solve6_device(S, x);
+            if (prm.trace && Ps.iters < prm.trace_cap)
+            {
+                IcpTrace &tr = prm.trace[(size_t)Ps.iters * P + pair];
+                for (int k = 0; k < 16; ++k)
+                    tr.T[k] = Ps.T[k];
+                for (int k = 0; k < kTerms; ++k)
+                    tr.S[k] = S[k];
+                for (int k = 0; k < 6; ++k)
+                    tr.x[k] = x[k];
+                tr.status = singular;
+            }
+            if (S[28] == 0.0)
+                Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
+            else if (singular && Ps.status == 0)
+                Ps.status = GCA3D_ERR_SINGULAR;
+            pose_from_x_device(x, prm.update_map, Ti);
+            double Tn[16];
+            for (int r = 0; r < 4; ++r)
+                for (int c = 0; c < 4; ++c)
+                {
+                    double v = 0.0;
+                    for (int k = 0; k < 4; ++k)
+                        v += Ti[4 * r + k] * Ps.T[4 * k + c];
+                    Tn[4 * r + c] = v;
+                }
+            for (int k = 0; k < 16; ++k)
+                Ps.T[k] = Tn[k];
+            Ps.iters += 1;
+            Ps.scale_iters[Ps.scale] += 1;
+            Ps.nn_warm = 1;
+            const double cth = 0.5 * (Ti[0] + Ti[5] + Ti[10] - 1.0);
+            const double tsq = Ti[3] * Ti[3] + Ti[7] * Ti[7] + Ti[11] * Ti[11];
+            if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
+            {
+                Ps.converged = 1;
+                Ps.active = 0;
+            }
         }
-        Ps.ticket = 0;
     }
-}
-
-// body of the device-side iteration loop: continue while a pair is still active and
-// the scale's iteration budget lasts
-__global__ void k_icp_loop_control(const PairState *st, int P, int *iter, int max_iter,
-                                   cudaGraphConditionalHandle handle)
-{
-    __shared__ int any;
+    if (!loop.iter)
+        return;
+    __threadfence();
+    __syncthreads();
     if (threadIdx.x == 0)
-        any = 0;
+        s_last = atomicAdd(loop.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last)
+        return;
+    __shared__ int s_any;
+    if (threadIdx.x == 0)
+        s_any = 0;
     __syncthreads();
     for (int p = threadIdx.x; p < P; p += blockDim.x)
-        if (st[p].active)
-            any = 1;
+        if (__ldcg(&st[p].active))
+            s_any = 1;
     __syncthreads();
     if (threadIdx.x == 0)
     {
-        const int it = ++(*iter);
-        cudaGraphSetConditional(handle, (any && it < max_iter) ? 1u : 0u);
+        *loop.ticket = 0u;
+        const int it = ++(*loop.iter);
+        cudaGraphSetConditional(loop.handle, (s_any && it < loop.max_iter) ? 1u : 0u);
     }
-}
-
-int icp_loop_control(gca3d_context *ctx, const PairState *st, int P, int *iter, int max_iter,
-                     cudaGraphConditionalHandle handle)
-{
-    k_icp_loop_control<<<1, 256, 0, ctx->stream>>>(st, P, iter, max_iter, handle);
-    GCA_CHECK_LAUNCH(ctx);
-    return GCA3D_OK;
 }
 
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
@@ -443,18 +450,28 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
 
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, const int *bmap, int max_blocks, const int *bmap_nn, int max_blocks_nn,
-                  double *partials, int2 *corr, const IcpScale &prm, bool compensated, int32_t *nn_out)
+                  double *partials, int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated,
+                  int32_t *nn_out, const IcpLoop *loop)
 {
+    const IcpLoop no_loop{};
+    const IcpLoop &L = loop ? *loop : no_loop;
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
     k_icp_nn<<<max_blocks_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P,
-                                                             prm.max_corr, corr, nn_out);
+                                                             prm.max_corr, corr, corr_prev, nn_out);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
         k_icp_accum<true><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
-                                                                       corr, st, bmap, src.P, partials, prm);
+                                                                       corr, st, bmap, src.P, partials,
+                                                                       prm.sqrt_lg, prm.sqrt_lc);
     else
         k_icp_accum<false><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0,
-                                                                        attr1, corr, st, bmap, src.P, partials, prm);
+                                                                        attr1, corr, st, bmap, src.P, partials,
+                                                                        prm.sqrt_lg, prm.sqrt_lc);
+    GCA_CHECK_LAUNCH(ctx);
+    if (compensated)
+        k_icp_finalize<true><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, partials, prm, L);
+    else
+        k_icp_finalize<false><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, partials, prm, L);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidIcpIter);
     return GCA3D_OK;

@@ -25,6 +25,7 @@ struct PairState
     int nsrc;
     int ntgt;
     int scale;
+    int nn_warm; // the correspondences of the previous iteration of this scale are valid
     int scale_iters[GCA3D_MAX_SCALES];
     int scale_nsrc[GCA3D_MAX_SCALES];
     int scale_ntgt[GCA3D_MAX_SCALES];
@@ -51,6 +52,17 @@ struct IcpScale
     int trace_cap = 0;
 };
 
+// the device-side iteration loop of a captured schedule: the finalize kernel's last
+// block counts the iteration and sets the WHILE node's condition (iter == nullptr:
+// no loop, eager launches)
+struct IcpLoop
+{
+    cudaGraphConditionalHandle handle = 0;
+    int *iter = nullptr;
+    unsigned *ticket = nullptr;
+    int max_iter = 0;
+};
+
 // the Gauss-Newton system for given correspondences (defined in icp.cu); the block
 // partials, the ticket and the count are scratch supplied by the caller
 __global__ void __launch_bounds__(kIcpThreads)
@@ -63,9 +75,8 @@ int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, 
               int *bmap_nn, int scale);
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, const int *bmap, int max_blocks, const int *bmap_nn, int max_blocks_nn,
-                  double *partials, int2 *corr, const IcpScale &prm, bool compensated, int32_t *nn_out);
-int icp_loop_control(gca3d_context *ctx, const PairState *st, int P, int *iter, int max_iter,
-                     cudaGraphConditionalHandle handle);
+                  double *partials, int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated,
+                  int32_t *nn_out, const IcpLoop *loop = nullptr);
 int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
              double *out30);
 int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,

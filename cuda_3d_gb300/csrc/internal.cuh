@@ -288,7 +288,8 @@ struct GridDev
     float *sint;   // intensity in sorted order
     int *scz;      // z cell in sorted order (compact copy for the in-row binary search)
     uint64_t *skey;
-    // row hash: key = (seg, cx, cy) -> [start, end) in one 16-byte slot
+    // row hash: key = (seg, cx, cy) -> [start, end) in one 16-byte slot; at least
+    // twice as many slots as points, so the first probe nearly always decides
     RowSlot *slots;
     uint32_t hmask;
     const int32_t *seg_off; // [P + 1] offsets of the segments in the sorted arrays

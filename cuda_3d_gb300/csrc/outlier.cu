@@ -42,6 +42,7 @@ __global__ void k_ror_flags(const float4 *__restrict__ pos, const int32_t *d_n, 
     const float cell = g.cell;
     const float rr = __fmul_rn(radius, radius);
     const int mx = (1 << L.bx) - 1, my = (1 << L.by) - 1;
+    const uint32_t hmask = g.hmask;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
     {
         const float4 p = pos[i];
@@ -58,13 +59,13 @@ __global__ void k_ror_flags(const float4 *__restrict__ pos, const int32_t *d_n, 
                 if (x < 0 || x > mx || y < 0 || y > my)
                     continue;
                 const unsigned long long rk = ((unsigned long long)x << L.by) | (unsigned long long)y;
-                const uint32_t h = hash_u64(rk) & g.hmask;
+                const uint32_t h = hash_u64(rk) & hmask;
                 const ulonglong2 v = slot_load(g.slots, h);
                 int2 r = make_int2(0, 0);
                 if (v.x == rk)
                     r = make_int2((int)(uint32_t)v.y, (int)(uint32_t)(v.y >> 32));
                 else if (v.x != kEmptyKey)
-                    r = row_probe_rest(g.slots, g.hmask, rk, h);
+                    r = row_probe_rest(g.slots, hmask, rk, h);
                 int a = r.x, b = r.y;
                 while (a < b) // first point of the row with z cell >= zlo
                 {

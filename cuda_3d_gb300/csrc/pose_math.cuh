@@ -293,11 +293,13 @@ __device__ __forceinline__ void gn_terms(float3 p, float Is, float3 q, float Iq,
     o.rc = slc * (Iproj - Is);
 }
 
-// FP32 pose (row-major 3x4) applied to a point
+// FP32 pose (row-major 3x4) applied to a point, as explicit fused multiply-adds
+// x' = fma(r0, x, fma(r1, y, fma(r2, z, t))) so that a CPU check can reproduce it
 __device__ __forceinline__ float3 apply_pose(const float *T, float4 s)
 {
-    return make_float3(T[0] * s.x + T[1] * s.y + T[2] * s.z + T[3], T[4] * s.x + T[5] * s.y + T[6] * s.z + T[7],
-                       T[8] * s.x + T[9] * s.y + T[10] * s.z + T[11]);
+    return make_float3(__fmaf_rn(T[0], s.x, __fmaf_rn(T[1], s.y, __fmaf_rn(T[2], s.z, T[3]))),
+                       __fmaf_rn(T[4], s.x, __fmaf_rn(T[5], s.y, __fmaf_rn(T[6], s.z, T[7]))),
+                       __fmaf_rn(T[8], s.x, __fmaf_rn(T[9], s.y, __fmaf_rn(T[10], s.z, T[11]))));
 }
 
 } // namespace gca3d

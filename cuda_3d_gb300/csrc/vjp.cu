@@ -327,7 +327,9 @@ extern "C" int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_c
     prm.trace_cap = K + 1;
     for (int k = 0; k <= K; ++k)
         if ((st = icp_iteration(ctx, bs, g, attr0, attr1, pst, bmap, max_blocks, bmap_nn, max_blocks_nn, partials,
-                                corr + (size_t)k * src->capacity, prm, true, d_corr ? d_corr + (size_t)k * ns : nullptr)))
+                                corr + (size_t)k * src->capacity,
+                                k ? corr + (size_t)(k - 1) * src->capacity : nullptr, prm, true,
+                                d_corr ? d_corr + (size_t)k * ns : nullptr)))
             return st;
 
     // backward

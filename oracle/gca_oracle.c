@@ -1930,3 +1930,17 @@ int64_t orc_radius_outlier_removal(const float *xyz, const float *rgb, int64_t n
     grid_free(&g);
     return m;
 }
+
+/* the GPU ICP kernels' FP32 pose application, x' = fma(r0, x, fma(r1, y, fma(r2, z, t)))
+ * with T the row-major 3x4 pose rounded to float */
+void orc_apply_pose_f32(const double T[16], const float *xyz, int64_t n, float *out)
+{
+    float t[12];
+    for (int k = 0; k < 12; ++k)
+        t[k] = (float)T[k];
+    for (int64_t i = 0; i < n; ++i) {
+        const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+        for (int r = 0; r < 3; ++r)
+            out[3 * i + r] = fmaf(t[4 * r], x, fmaf(t[4 * r + 1], y, fmaf(t[4 * r + 2], z, t[4 * r + 3])));
+    }
+}

@@ -172,6 +172,10 @@ typedef struct {
     int update_map;
 } orc_unroll_params;
 
+/* the GPU ICP kernels' FP32 pose application: fused multiply-adds in the order
+ * fma(r0, x, fma(r1, y, fma(r2, z, t))), T rounded to float (row-major 4x4 in) */
+void orc_apply_pose_f32(const double T[16], const float *xyz, int64_t n, float *out);
+
 /* dU/dx_m as 3x4 row-major blocks for U = pose map(x) */
 void orc_pose_jacobian(const double x[6], int update_map, double dU[6][12]);
 

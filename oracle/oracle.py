@@ -97,6 +97,7 @@ def _bind(L):
         "orc_color_icp_ref32": (v, [F32, F32, i64, F32, F32, F32, F32, i64, C.c_int, C.c_float,
                                     F32, C.POINTER(IcpResult)]),
         "orc_pose_jacobian": (v, [F64, C.c_int, F64]),
+        "orc_apply_pose_f32": (v, [F64, F32, i64, F32]),
         "orc_radius_outlier_removal": (i64, [F32, F32, i64, C.c_float, C.c_int, F32, F32]),
         "orc_icp_unrolled_f64": (C.c_double, [F64, F64, i64, F32, F32, F64, F64, i64,
                                               C.POINTER(UnrollParams), F64, C.c_void_p, C.c_void_p, F64]),
@@ -360,6 +361,14 @@ def multiscale_ref32(src_xyz, src_rgb, tgt_xyz, tgt_rgb, scales, T_init=None):
 # K unrolled Gauss-Newton steps and their adjoint (FP64; no reference
 # counterpart).  T_0 = Exp(xi0); corr is (K + 1) x ns target indices.
 # --------------------------------------------------------------------------- #
+def apply_pose_f32(T, xyz):
+    """the GPU ICP kernels' FP32 transform of points (fused, in a fixed order)"""
+    xyz = _f32(xyz)
+    out = np.empty_like(xyz)
+    lib().orc_apply_pose_f32(np.ascontiguousarray(T, np.float64).reshape(-1), xyz, len(xyz), out)
+    return out
+
+
 def pose_jacobian(x, update_map=UPDATE_SE3_EXP):
     d = np.zeros(72, np.float64)
     lib().orc_pose_jacobian(np.ascontiguousarray(x, np.float64), int(update_map), d)

@@ -218,3 +218,20 @@ def test_vjp_rejects_bad_arguments(ctx, N, c2):
     st = ctx.L.gca3d_color_icp_vjp(ctx.h, c2["src"].h, c2["tgt"].h, C.byref(ok), x0.ctypes.data, G.ctypes.data, 0.0,
                                    None, None, None, None, None, None)
     assert st == N.ERR_INVALID_VALUE
+
+
+def test_pruned_correspondences_are_exact(ctx, N, orc, c2):
+    """From the second evaluation of a scale on, the ICP correspondence search is
+    shrunk to the ball around the previous correspondence.  The correspondences of
+    evaluations 1..K must equal an exhaustive nearest-neighbour search (ties to the
+    smaller index) at the same FP32 points, reproduced on the CPU from T_k."""
+    K = 4
+    pr = c2["pr"]
+    r = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], c2["xi0"], K=K, max_corr=MAX_CORR, want_corr=True)
+    sx = np.asarray(pr.src_xyz, np.float32)
+    tx = np.asarray(pr.tgt_xyz, np.float32)
+    for k in range(1, K + 1):
+        Tk = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], c2["xi0"], K=k, max_corr=MAX_CORR)["T"]
+        p = orc.apply_pose_f32(Tk, sx)
+        nn = orc.nn_search(p, tx, MAX_CORR, tie=orc.TIE_MIN_INDEX)
+        np.testing.assert_array_equal(r["corr"][k], nn)
