@@ -163,6 +163,7 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
         bmap_nn[p] = bn;
         bn += (ns > 0 && nt > 0) ? (ns + kNNChunk - 1) / kNNChunk : 0;
         S.nblocks = nb;
+        S.nblocks_nn = (ns > 0 && nt > 0) ? (ns + kNNChunk - 1) / kNNChunk : 0;
         S.nsrc = ns;
         S.ntgt = nt;
         S.ticket = 0;
@@ -201,18 +202,22 @@ __global__ void k_state_init(PairState *st, int P, const double *T_init)
     st[p].rmse_ref = st[p].fitness = st[p].inlier_rmse = 0.0;
 }
 
-// block -> (pair, chunk) of the pair's source points; pose as FP32 in shared memory
+// work item w -> (pair, chunk) of the pair's source points; the pair's pose as
+// FP32 in shared memory.  Every thread of the block must call it (it synchronises).
+// Blocks take items in a strided order, so blocks running at the same time work
+// on neighbouring points and share their target rows in L2.
 struct BlockPair
 {
     int pair, start, end;
 };
 
-__device__ __forceinline__ BlockPair block_pair(const int32_t *src_off, const PairState *st, const int *bmap, int P,
-                                                int chunk, float *s_T, int *s_pair)
+__device__ __forceinline__ BlockPair item_pair(int w, const int32_t *src_off, const PairState *st, const int *bmap,
+                                               int P, int chunk, float *s_T, int *s_pair)
 {
+    __syncthreads(); // the previous item's readers of s_T / s_pair are done
     if (threadIdx.x == 0)
     {
-        int p = find_pair(bmap, P, blockIdx.x);
+        int p = find_pair(bmap, P, w);
         if (p >= 0 && !st[p].active)
             p = -1;
         *s_pair = p;
@@ -223,9 +228,10 @@ __device__ __forceinline__ BlockPair block_pair(const int32_t *src_off, const Pa
     __syncthreads();
     BlockPair b;
     b.pair = *s_pair;
+    b.start = b.end = 0;
     if (b.pair >= 0)
     {
-        b.start = src_off[b.pair] + (blockIdx.x - bmap[b.pair]) * chunk;
+        b.start = src_off[b.pair] + (w - bmap[b.pair]) * chunk;
         b.end = min(b.start + chunk, src_off[b.pair + 1]);
     }
     return b;
@@ -243,12 +249,15 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
-    const BlockPair b = block_pair(src_off, st, bmap, P, kNNChunk, s_T, &s_pair);
-    if (b.pair < 0)
-        return;
     const KeyLayout L = *g.layout;
-    const float3 o = g.gmin[b.pair];
     const float rr = __fmul_rn(max_corr, max_corr);
+    const int items = bmap[P];
+    for (int w = blockIdx.x; w < items; w += gridDim.x)
+    {
+    const BlockPair b = item_pair(w, src_off, st, bmap, P, kNNChunk, s_T, &s_pair);
+    if (b.pair < 0)
+        continue;
+    const float3 o = g.gmin[b.pair];
     const int tbase = g.seg_off[b.pair];
     const bool warm = corr_prev && st[b.pair].nn_warm;
     // four lanes per source point (uniform trip count for the whole block)
@@ -278,6 +287,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
                 nn_out[i] = best.t >= 0 ? __ldg(&g.sidx[best.t]) - tbase : -1;
         }
     }
+    }
 }
 
 // step 2: residuals, Jacobians, block sums (one partial per block)
@@ -292,9 +302,12 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restr
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
-    const BlockPair b = block_pair(src_off, st, bmap, P, kIcpChunk, s_T, &s_pair);
+    const int items = bmap[P];
+    for (int w = blockIdx.x; w < items; w += gridDim.x)
+    {
+    const BlockPair b = item_pair(w, src_off, st, bmap, P, kIcpChunk, s_T, &s_pair);
     if (b.pair < 0)
-        return;
+        continue;
     Acc<Comp> acc;
     acc.zero();
     for (int i = b.start + threadIdx.x; i < b.end; i += kIcpThreads)
@@ -312,7 +325,8 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restr
                  make_float3(a1.x, a1.y, a1.z), slg, slc, terms);
         acc.add_terms(terms, __int_as_float(c.y));
     }
-    block_reduce_store<Comp>(acc, partials + (size_t)blockIdx.x * kTermsPad);
+    block_reduce_store<Comp>(acc, partials + (size_t)w * kTermsPad);
+    }
 }
 
 // step 3, one block per pair: the pair's block partials summed in FP64 in block
@@ -321,7 +335,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restr
 // decides whether the device-side iteration loop goes on: while a pair is active
 // and the scale's budget lasts.
 template <bool Comp>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int P, const int *bmap,
+__global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int P, int *bmap, int *bmap_nn,
                                                               const double *partials, IcpScale prm, IcpLoop loop)
 {
     const int pair = blockIdx.x;
@@ -347,22 +361,27 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
             s_red[grp][lane] = Comp ? v : (double)vf;
         }
         __syncthreads();
+        __shared__ double s_S[kTermsPad];
+        if (threadIdx.x < kTerms)
+        {
+            const int k = threadIdx.x;
+            double v = 0.0;
+            float vf = 0.0f;
+            for (int w = 0; w < kIcpThreads / 32; ++w)
+            {
+                if (Comp)
+                    v += s_red[w][k];
+                else
+                    vf += (float)s_red[w][k];
+            }
+            s_S[k] = Comp ? v : (double)vf;
+        }
+        __syncthreads();
         if (threadIdx.x == 0)
         {
             double S[kTerms];
             for (int k = 0; k < kTerms; ++k)
-            {
-                double v = 0.0;
-                float vf = 0.0f;
-                for (int w = 0; w < kIcpThreads / 32; ++w)
-                {
-                    if (Comp)
-                        v += s_red[w][k];
-                    else
-                        vf += (float)s_red[w][k];
-                }
-                S[k] = Comp ? v : (double)vf;
-            }
+                S[k] = s_S[k];
             const double ns = (double)Ps.nsrc;
             Ps.rmse_ref = S[27] / ns;
             Ps.fitness = S[28] / ns;
@@ -408,8 +427,9 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
             }
         }
     }
-    if (!loop.iter)
-        return;
+    // the last block: work maps over the pairs still active (the next iteration's
+    // NN and accumulate launches get no items for converged pairs) and, in a
+    // captured schedule, the loop condition
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0)
@@ -417,19 +437,49 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
     __syncthreads();
     if (!s_last)
         return;
-    __shared__ int s_any;
-    if (threadIdx.x == 0)
-        s_any = 0;
-    __syncthreads();
-    for (int p = threadIdx.x; p < P; p += blockDim.x)
-        if (__ldcg(&st[p].active))
-            s_any = 1;
+    __shared__ int s_sum[kIcpThreads], s_sum_nn[kIcpThreads];
+    const int per = (P + kIcpThreads - 1) / kIcpThreads;
+    const int p0 = min(P, (int)threadIdx.x * per), p1 = min(P, p0 + per);
+    int a = 0, an = 0;
+    for (int q = p0; q < p1; ++q)
+        if (__ldcg(&st[q].active))
+        {
+            a += st[q].nblocks;
+            an += st[q].nblocks_nn;
+        }
+    s_sum[threadIdx.x] = a;
+    s_sum_nn[threadIdx.x] = an;
     __syncthreads();
     if (threadIdx.x == 0)
     {
+        int x = 0, y = 0;
+        for (int k = 0; k < kIcpThreads; ++k)
+        {
+            const int u = s_sum[k], v = s_sum_nn[k];
+            s_sum[k] = x, s_sum_nn[k] = y;
+            x += u, y += v;
+        }
+        bmap[P] = x;
+        bmap_nn[P] = y;
         *loop.ticket = 0u;
-        const int it = ++(*loop.iter);
-        cudaGraphSetConditional(loop.handle, (s_any && it < loop.max_iter) ? 1u : 0u);
+        if (loop.iter)
+        {
+            const int it = ++(*loop.iter);
+            cudaGraphSetConditional(loop.handle, (y > 0 && it < loop.max_iter) ? 1u : 0u);
+        }
+    }
+    __syncthreads();
+    a = s_sum[threadIdx.x];
+    an = s_sum_nn[threadIdx.x];
+    for (int q = p0; q < p1; ++q)
+    {
+        bmap[q] = a;
+        bmap_nn[q] = an;
+        if (__ldcg(&st[q].active))
+        {
+            a += st[q].nblocks;
+            an += st[q].nblocks_nn;
+        }
     }
 }
 
@@ -449,29 +499,33 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
 }
 
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
-                  PairState *st, const int *bmap, int max_blocks, const int *bmap_nn, int max_blocks_nn,
-                  double *partials, int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated,
-                  int32_t *nn_out, const IcpLoop *loop)
+                  PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
+                  int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated, int32_t *nn_out,
+                  const IcpLoop &loop)
 {
-    const IcpLoop no_loop{};
-    const IcpLoop &L = loop ? *loop : no_loop;
+    if (!loop.ticket)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: iteration without a finalize ticket");
+    // work-item loops: enough blocks to fill the SMs a few times over, never more
+    // than the items the capacity can produce
+    const int grid_nn = std::max(std::min(max_blocks_nn, ctx->num_sms * 10), 1);
+    const int grid_acc = std::max(std::min(max_blocks, ctx->num_sms * 6), 1);
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
-    k_icp_nn<<<max_blocks_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P,
-                                                             prm.max_corr, corr, corr_prev, nn_out);
+    k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
+                                                       corr, corr_prev, nn_out);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
-        k_icp_accum<true><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
-                                                                       corr, st, bmap, src.P, partials,
-                                                                       prm.sqrt_lg, prm.sqrt_lc);
+        k_icp_accum<true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
+                                                                     corr, st, bmap, src.P, partials, prm.sqrt_lg,
+                                                                     prm.sqrt_lc);
     else
-        k_icp_accum<false><<<max_blocks, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0,
-                                                                        attr1, corr, st, bmap, src.P, partials,
-                                                                        prm.sqrt_lg, prm.sqrt_lc);
+        k_icp_accum<false><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
+                                                                      corr, st, bmap, src.P, partials, prm.sqrt_lg,
+                                                                      prm.sqrt_lc);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
-        k_icp_finalize<true><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, partials, prm, L);
+        k_icp_finalize<true><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm, loop);
     else
-        k_icp_finalize<false><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, partials, prm, L);
+        k_icp_finalize<false><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm, loop);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidIcpIter);
     return GCA3D_OK;

@@ -7,8 +7,8 @@ namespace gca3d
 {
 
 constexpr int kIcpThreads = 256;
-constexpr int kIcpChunk = 1024; // source points per accumulate block (one partial each)
-constexpr int kNNChunk = 256;   // source points per NN block (many short blocks hide latency)
+constexpr int kIcpChunk = 1024; // source points per accumulate work item (one partial each)
+constexpr int kNNChunk = 256;   // source points per correspondence work item
 constexpr int kTerms = 30;      // 21 JTJ (upper) + 6 JTr + r^2 + correspondences + sum d^2
 constexpr int kTermsPad = 32;
 
@@ -21,7 +21,8 @@ struct PairState
     int active;
     int status;
     unsigned int ticket;
-    int nblocks;
+    int nblocks;    // accumulate work items (kIcpChunk points) of the scale
+    int nblocks_nn; // correspondence work items (kNNChunk points) of the scale
     int nsrc;
     int ntgt;
     int scale;
@@ -52,9 +53,10 @@ struct IcpScale
     int trace_cap = 0;
 };
 
-// the device-side iteration loop of a captured schedule: the finalize kernel's last
-// block counts the iteration and sets the WHILE node's condition (iter == nullptr:
-// no loop, eager launches)
+// control of one iteration: the finalize kernel's blocks take a ticket (zero
+// before the first iteration); the last one rebuilds the work maps and, in a
+// captured schedule (iter set), counts the iteration and sets the WHILE node's
+// condition
 struct IcpLoop
 {
     cudaGraphConditionalHandle handle = 0;
@@ -74,9 +76,9 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
               int *bmap_nn, int scale);
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
-                  PairState *st, const int *bmap, int max_blocks, const int *bmap_nn, int max_blocks_nn,
-                  double *partials, int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated,
-                  int32_t *nn_out, const IcpLoop *loop = nullptr);
+                  PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
+                  int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated, int32_t *nn_out,
+                  const IcpLoop &loop);
 int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
              double *out30);
 int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,

@@ -73,8 +73,10 @@ __device__ inline int solve6_device(const double *S /* 21 upper + 6 rhs */, doub
                 A[i][k] = 0.0;
             continue;
         }
+        // one reciprocal per pivot: FP64 division is a long dependent sequence here
+        const double inv = 1.0 / D[k];
         for (int i = k + 1; i < 6; ++i)
-            A[i][k] /= D[k];
+            A[i][k] *= inv;
         for (int i = k + 1; i < 6; ++i)
             for (int j = k + 1; j <= i; ++j)
             {

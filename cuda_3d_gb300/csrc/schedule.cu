@@ -159,15 +159,17 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         prm.update_map = p.update_map;
         prm.rot_eps = p.rot_eps;
         prm.trans_eps = p.trans_eps;
-        // loop counter and finalize ticket of the captured loop (same arena layout eager)
+        // loop counter and finalize ticket
         int *iter = ctx->arena.get<int>(2);
         if (!iter)
             return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
+        GCA_CUDA(ctx, cudaMemsetAsync(iter, 0, 2 * sizeof(int), ctx->stream));
+        IcpLoop loop;
+        loop.ticket = reinterpret_cast<unsigned *>(iter + 1);
         if (capturing && S.max_iter > 0)
         {
             // the iteration loop as a device-side WHILE node: the body runs while a
             // pair is active and the budget lasts, so converged schedules stop early
-            GCA_CUDA(ctx, cudaMemsetAsync(iter, 0, 2 * sizeof(int), ctx->stream));
             cudaStreamCaptureStatus cs;
             cudaGraph_t cg = nullptr;
             const cudaGraphNode_t *deps = nullptr;
@@ -188,13 +190,11 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
                                                         cudaStreamCaptureModeThreadLocal));
             ctx->stream = pl->side;
             const int64_t l0 = ctx->launches;
-            IcpLoop loop;
             loop.handle = handle;
             loop.iter = iter;
-            loop.ticket = reinterpret_cast<unsigned *>(iter + 1);
             loop.max_iter = S.max_iter;
             st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                               pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr, &loop);
+                               pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr, loop);
             pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
             ctx->stream = main_stream;
             cudaGraph_t captured = nullptr;
@@ -209,7 +209,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         for (int it = 0; it < S.max_iter; ++it)
         {
             if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                                    pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr)))
+                                    pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr,
+                                    loop)))
                 return st;
             if (pl->host_checks && !capturing)
             {
