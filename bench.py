@@ -65,6 +65,7 @@ def parse_args(argv=None):
                    "for profilers that do not descend into conditional graph nodes)")
     p.add_argument("--no-extras", action="store_true", help="skip the per-row measurements (frame pair, "
                    "single pair, adjoint, stream)")
+    p.add_argument("--no-tune", action="store_true", help="default launch shape instead of the autotuner's")
     p.add_argument("--stream-frames", type=int, default=200, help="frames of the 640x480 stream (720p: half)")
     return p.parse_args(argv)
 
@@ -248,6 +249,15 @@ def run_ours(args):
     scales = [N.scale(*s) for s in SCALES]
     chosen = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True,
                           use_graph=not (args.quick and args.eager))
+    # launch shape from the autotuner (outside every timed region; results do not depend on it)
+    tuning, tune_ms = None, None
+    if not args.no_tune and not args.quick:
+        t0 = time.perf_counter()
+        best, best_ms = N.icp_autotune(ctx, srcs, tgts, chosen, reps=2)
+        chosen.tuning = best
+        tuning = {"nn_item_points": best.nn_item_points, "nn_blocks_per_sm": best.nn_blocks_per_sm,
+                  "accum_blocks_per_sm": best.accum_blocks_per_sm, "ms_per_execute": best_ms,
+                  "search_s": time.perf_counter() - t0}
     plan = N.IcpPlan(ctx, srcs, tgts, chosen)
     res_chosen = None
     for _ in range(max(args.warmup, 3)):
@@ -312,7 +322,8 @@ def run_ours(args):
            "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e}
 
     # ---- roofline of the ICP iteration kernel (eager run, CUDA events) ---------
-    prof = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True, use_graph=False)
+    prof = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=True, use_graph=False,
+                        tuning=chosen.tuning)
     plan_prof = N.IcpPlan(ctx, srcs, tgts, prof)
     plan_prof.execute(results=True)
     ctx.profile_begin("icp_iter")
@@ -370,6 +381,7 @@ def run_ours(args):
                                "trans 0-15 cm, overlap 40-90 %, scales voxel 0.04/0.02/0.01 m x 50/30/14 iterations",
                    "pairs_per_gpu": P, "src_points": n_src, "tgt_points": n_tgt,
                    "scales": SCALES, "parallelism": f"replicas x{world} (pairs sharded per rank)",
+                   "tuning": tuning,
                    "l2": f"inputs larger than L2 ({(n_src + n_tgt) * 32 / 1e6:.0f} MB resident SoA)"},
         "e2e": e2e,
         "roofline": roofline,

@@ -146,7 +146,7 @@ __device__ __forceinline__ int find_pair(const int *bmap, int P, int b)
 
 // per-scale setup: block map, per-pair counts, reset of the per-scale flags
 __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-                            int *bmap_nn, int scale)
+                            int *bmap_nn, int scale, int nn_chunk)
 {
     if (threadIdx.x != 0)
         return;
@@ -161,9 +161,9 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
         bmap[p] = b;
         b += nb;
         bmap_nn[p] = bn;
-        bn += (ns > 0 && nt > 0) ? (ns + kNNChunk - 1) / kNNChunk : 0;
+        bn += (ns > 0 && nt > 0) ? (ns + nn_chunk - 1) / nn_chunk : 0;
         S.nblocks = nb;
-        S.nblocks_nn = (ns > 0 && nt > 0) ? (ns + kNNChunk - 1) / kNNChunk : 0;
+        S.nblocks_nn = (ns > 0 && nt > 0) ? (ns + nn_chunk - 1) / nn_chunk : 0;
         S.nsrc = ns;
         S.ntgt = nt;
         S.ticket = 0;
@@ -245,7 +245,7 @@ __device__ __forceinline__ BlockPair item_pair(int w, const int32_t *src_off, co
 __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                         GridDev g, const PairState *st, const int *bmap, int P,
                                                         float max_corr, int2 *corr, const int2 *corr_prev,
-                                                        int32_t *nn_out)
+                                                        int32_t *nn_out, int nn_chunk)
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
     const int items = bmap[P];
     for (int w = blockIdx.x; w < items; w += gridDim.x)
     {
-    const BlockPair b = item_pair(w, src_off, st, bmap, P, kNNChunk, s_T, &s_pair);
+    const BlockPair b = item_pair(w, src_off, st, bmap, P, nn_chunk, s_T, &s_pair);
     if (b.pair < 0)
         continue;
     const float3 o = g.gmin[b.pair];
@@ -483,10 +483,22 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
     }
 }
 
-int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-              int *bmap_nn, int scale)
+IcpShape icp_shape(const gca3d_tuning &t)
 {
-    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, bmap_nn, scale);
+    IcpShape s;
+    if (t.nn_item_points == 64 || t.nn_item_points == 128 || t.nn_item_points == 256 || t.nn_item_points == 512)
+        s.nn_chunk = t.nn_item_points;
+    if (t.nn_blocks_per_sm > 0)
+        s.nn_bps = std::min(t.nn_blocks_per_sm, 64);
+    if (t.accum_blocks_per_sm > 0)
+        s.acc_bps = std::min(t.accum_blocks_per_sm, 64);
+    return s;
+}
+
+int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
+              int *bmap_nn, int scale, int nn_chunk)
+{
+    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, bmap_nn, scale, nn_chunk);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
@@ -501,17 +513,17 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
                   int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated, int32_t *nn_out,
-                  const IcpLoop &loop)
+                  const IcpLoop &loop, const IcpShape &shape)
 {
     if (!loop.ticket)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: iteration without a finalize ticket");
     // work-item loops: enough blocks to fill the SMs a few times over, never more
     // than the items the capacity can produce
-    const int grid_nn = std::max(std::min(max_blocks_nn, ctx->num_sms * 10), 1);
-    const int grid_acc = std::max(std::min(max_blocks, ctx->num_sms * 6), 1);
+    const int grid_nn = std::max(std::min(max_blocks_nn, ctx->num_sms * shape.nn_bps), 1);
+    const int grid_acc = std::max(std::min(max_blocks, ctx->num_sms * shape.acc_bps), 1);
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
     k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
-                                                       corr, corr_prev, nn_out);
+                                                       corr, corr_prev, nn_out, shape.nn_chunk);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
         k_icp_accum<true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,

@@ -8,7 +8,17 @@ namespace gca3d
 
 constexpr int kIcpThreads = 256;
 constexpr int kIcpChunk = 1024; // source points per accumulate work item (one partial each)
-constexpr int kNNChunk = 256;   // source points per correspondence work item
+constexpr int kNNChunk = 256;   // default source points per correspondence work item
+constexpr int kNNChunkMin = 64; // the smallest item size a tuning may choose
+
+// the launch shape in force (defaults filled in)
+struct IcpShape
+{
+    int nn_chunk = kNNChunk;
+    int nn_bps = 10;
+    int acc_bps = 6;
+};
+IcpShape icp_shape(const gca3d_tuning &t);
 constexpr int kTerms = 30;      // 21 JTJ (upper) + 6 JTr + r^2 + correspondences + sum d^2
 constexpr int kTermsPad = 32;
 
@@ -74,11 +84,11 @@ __global__ void __launch_bounds__(kIcpThreads)
 
 int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit);
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-              int *bmap_nn, int scale);
+              int *bmap_nn, int scale, int nn_chunk);
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
                   int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated, int32_t *nn_out,
-                  const IcpLoop &loop);
+                  const IcpLoop &loop, const IcpShape &shape);
 int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
              double *out30);
 int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,

@@ -150,7 +150,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         else if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
                                      keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
             return st;
-        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, bmap_nn, si)))
+        const IcpShape shape = icp_shape(p.tuning);
+        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, bmap_nn, si, shape.nn_chunk)))
             return st;
         IcpScale prm;
         prm.max_corr = S.max_corr;
@@ -194,7 +195,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             loop.iter = iter;
             loop.max_iter = S.max_iter;
             st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                               pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr, loop);
+                               pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr, loop,
+                               shape);
             pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
             ctx->stream = main_stream;
             cudaGraph_t captured = nullptr;
@@ -210,7 +212,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         {
             if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
                                     pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr,
-                                    loop)))
+                                    loop, shape)))
                 return st;
             if (pl->host_checks && !capturing)
             {
@@ -334,7 +336,7 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
         pl->src_max = std::max(pl->src_max, src[k]->capacity);
         pl->tgt_max = std::max(pl->tgt_max, tgt[k]->capacity);
         nb += div_up(src[k]->capacity, kIcpChunk);
-        pl->max_blocks_nn += div_up(src[k]->capacity, kNNChunk);
+        pl->max_blocks_nn += div_up(src[k]->capacity, icp_shape(params->tuning).nn_chunk);
     }
     pl->max_blocks = std::max(nb, 1);
     pl->max_blocks_nn = std::max(pl->max_blocks_nn, 1);
@@ -497,3 +499,89 @@ int gca3d_color_icp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt, cons
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------
+// launch-shape autotuner: coordinate descent over the knobs of gca3d_tuning, each
+// candidate timed on the caller's workload as a fresh plan (one warm-up execute,
+// then `reps` executes between CUDA events on the context stream)
+// ---------------------------------------------------------------------------
+extern "C" int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
+                                  const gca3d_icp_params *params, int reps, gca3d_tuning *best, double *best_ms)
+{
+    if (!ctx || !params || !src || !tgt || n_pairs < 1)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "autotune: bad arguments");
+    reps = std::max(reps, 1);
+    gca3d_icp_params p = *params;
+    const IcpShape s0 = icp_shape(p.tuning);
+    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    {
+        cudaGetLastError();
+        if (e0)
+            cudaEventDestroy(e0);
+        return fail(ctx, GCA3D_ERR_CUDA, "autotune: events");
+    }
+    auto time_one = [&](const gca3d_tuning &t, double &ms) -> int {
+        p.tuning = t;
+        gca3d_icp_plan *pl = nullptr;
+        int st = icp_plan_create_internal(ctx, n_pairs, src, tgt, &p, p.use_graph != 0, nullptr, &pl);
+        if (st)
+            return st;
+        st = gca3d_icp_plan_execute(pl, nullptr, nullptr);
+        if (!st && cudaEventRecord(e0, ctx->stream) != cudaSuccess)
+            st = cuda_fail(ctx, cudaGetLastError(), "autotune: event");
+        for (int r = 0; r < reps && !st; ++r)
+            st = gca3d_icp_plan_execute(pl, nullptr, nullptr);
+        if (!st)
+        {
+            cudaError_t e = cudaEventRecord(e1, ctx->stream);
+            if (e == cudaSuccess)
+                e = cudaEventSynchronize(e1);
+            float f = 0.0f;
+            if (e == cudaSuccess)
+                e = cudaEventElapsedTime(&f, e0, e1);
+            if (e != cudaSuccess)
+                st = cuda_fail(ctx, e, "autotune: timing");
+            ms = (double)f / reps;
+        }
+        gca3d_icp_plan_destroy(pl);
+        if (!st)
+            st = consume_device_error(ctx, "autotune");
+        return st;
+    };
+    double best_t = 0.0;
+    int st = time_one(cur, best_t);
+    const int nn_items[] = {64, 128, 256, 512};
+    const int nn_bps[] = {4, 6, 8, 10, 14, 20};
+    const int acc_bps[] = {2, 3, 4, 6, 8, 12};
+    for (int knob = 0; knob < 3 && !st; ++knob)
+    {
+        const int *vals = knob == 0 ? nn_items : (knob == 1 ? nn_bps : acc_bps);
+        const int nv = knob == 0 ? 4 : 6;
+        for (int v = 0; v < nv && !st; ++v)
+        {
+            gca3d_tuning t = cur;
+            int &field = knob == 0 ? t.nn_item_points : (knob == 1 ? t.nn_blocks_per_sm : t.accum_blocks_per_sm);
+            if (field == vals[v])
+                continue;
+            field = vals[v];
+            double ms = 0.0;
+            st = time_one(t, ms);
+            if (!st && ms < best_t)
+            {
+                best_t = ms;
+                cur = t;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st)
+        return st;
+    if (best)
+        *best = cur;
+    if (best_ms)
+        *best_ms = best_t;
+    return GCA3D_OK;
+}

@@ -315,7 +315,8 @@ extern "C" int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_c
         return st;
     k_vjp_init<<<1, 32, 0, ctx->stream>>>(pst, x0);
     GCA_CHECK_LAUNCH(ctx);
-    if ((st = icp_setup(ctx, pst, 1, bs.seg_off, bt.seg_off, bmap, bmap_nn, 0)))
+    const IcpShape shape;
+    if ((st = icp_setup(ctx, pst, 1, bs.seg_off, bt.seg_off, bmap, bmap_nn, 0, shape.nn_chunk)))
         return st;
     IcpScale prm;
     prm.max_corr = p->max_corr;
@@ -333,7 +334,7 @@ extern "C" int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_c
         if ((st = icp_iteration(ctx, bs, g, attr0, attr1, pst, bmap, max_blocks, bmap_nn, max_blocks_nn, partials,
                                 corr + (size_t)k * src->capacity,
                                 k ? corr + (size_t)(k - 1) * src->capacity : nullptr, prm, true,
-                                d_corr ? d_corr + (size_t)k * ns : nullptr, loop)))
+                                d_corr ? d_corr + (size_t)k * ns : nullptr, loop, shape)))
             return st;
 
     // backward

@@ -47,10 +47,15 @@ class ScaleParams(C.Structure):
                 ("normal_radius", C.c_float), ("grad_radius", C.c_float), ("max_nn", C.c_int)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("nn_item_points", C.c_int), ("nn_blocks_per_sm", C.c_int), ("accum_blocks_per_sm", C.c_int)]
+
+
 class IcpParams(C.Structure):
     _fields_ = [("n_scales", C.c_int), ("scales", ScaleParams * MAX_SCALES), ("lambda_", C.c_float),
                 ("update_map", C.c_int), ("rot_eps", C.c_double), ("trans_eps", C.c_double),
-                ("compensated", C.c_int), ("use_graph", C.c_int), ("keep_target_normals", C.c_int)]
+                ("compensated", C.c_int), ("use_graph", C.c_int), ("keep_target_normals", C.c_int),
+                ("tuning", Tuning)]
 
 
 class IcpResult(C.Structure):
@@ -117,6 +122,8 @@ _SIGS = {
     "gca3d_icp_plan_execute": [_P, _P, _P],
     "gca3d_icp_plan_destroy": [_P],
     "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
+    "gca3d_icp_autotune": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), C.c_int, C.POINTER(Tuning),
+                           C.POINTER(C.c_double)],
     "gca3d_radius_outlier_removal": [_P, _P, _F, C.c_int, _P],
     "gca3d_cloud_select": [_P, _P, _P, _I64, _P],
     "gca3d_cloud_to_aos": [_P, _P, _P, _P],
@@ -303,7 +310,7 @@ def scale(voxel, max_iter, max_corr, normal_radius, grad_radius, max_nn=0):
 
 
 def icp_params(scales, lam=0.968, update_map=UPDATE_EULER_ZYX, rot_eps=1e-6, trans_eps=1e-6, compensated=True,
-               use_graph=False, keep_target_normals=False):
+               use_graph=False, keep_target_normals=False, tuning=None):
     p = IcpParams()
     p.n_scales = len(scales)
     for i, s in enumerate(scales):
@@ -315,7 +322,17 @@ def icp_params(scales, lam=0.968, update_map=UPDATE_EULER_ZYX, rot_eps=1e-6, tra
     p.compensated = int(compensated)
     p.use_graph = int(use_graph)
     p.keep_target_normals = int(keep_target_normals)
+    if tuning is not None:
+        p.tuning = tuning if isinstance(tuning, Tuning) else Tuning(*tuning)
     return p
+
+
+def icp_autotune(ctx, srcs, tgts, params, reps=3):
+    """the fastest launch shape for this workload: (Tuning, ms per execute)"""
+    best, ms = Tuning(), C.c_double()
+    ctx.check(ctx.L.gca3d_icp_autotune(ctx.h, len(srcs), cloud_array(srcs), cloud_array(tgts), C.byref(params),
+                                       int(reps), C.byref(best), C.byref(ms)))
+    return best, ms.value
 
 
 def result_dict(r):

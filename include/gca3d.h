@@ -80,6 +80,14 @@ typedef struct {
     int max_nn; /* 0 = every neighbour inside normal_radius (reference) */
 } gca3d_scale;
 
+/* launch shape of the ICP iterations (0 = default).  Only the shape changes: results are
+ * bit-identical for every setting.  gca3d_icp_autotune picks one for a workload. */
+typedef struct {
+    int nn_item_points;      /* source points per correspondence work item: 64, 128, 256 (default), 512 */
+    int nn_blocks_per_sm;    /* correspondence grid = SMs x this (default 10), at most the items */
+    int accum_blocks_per_sm; /* accumulate grid = SMs x this (default 6), at most the items */
+} gca3d_tuning;
+
 typedef struct {
     int n_scales;
     gca3d_scale scales[GCA3D_MAX_SCALES];
@@ -90,6 +98,7 @@ typedef struct {
     int compensated;   /* 1: Kahan FP32 in each block, FP64 across blocks; 0: plain FP32 */
     int use_graph;     /* 1: replay the whole schedule as one CUDA graph */
     int keep_target_normals; /* 1 with voxel <= 0: use the normals already on the target */
+    gca3d_tuning tuning;
 } gca3d_icp_params;
 
 typedef struct {
@@ -292,6 +301,14 @@ int gca3d_icp_plan_execute(gca3d_icp_plan *plan, const double *T_init,
 int gca3d_icp_plan_destroy(gca3d_icp_plan *plan);
 /* kernels one execute launches (graph nodes, or the eager launches of the last run) */
 int gca3d_icp_plan_kernels(gca3d_icp_plan *plan, int64_t *n);
+
+/* time candidate launch shapes on this workload (plans built as params say, each executed
+ * `reps` times after one warm-up, CUDA events on the context stream) by coordinate descent
+ * from the defaults; writes the fastest to *best and its time per execute to *best_ms
+ * (either may be NULL).  params->tuning is the starting point when set. */
+int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src,
+                       gca3d_cloud *const *tgt, const gca3d_icp_params *params, int reps,
+                       gca3d_tuning *best, double *best_ms);
 
 /* ---------------------------------------------------------------------------
  * frame-to-frame tracking of an RGB-D stream (the reference's demo loop,

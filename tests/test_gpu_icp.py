@@ -219,3 +219,22 @@ def test_frame_pair_pipeline_vs_oracle(ctx, N, orc, synth):
     r3 = N.color_icp(ctx, src, tgt, N.icp_params(sc3, update_map=N.UPDATE_SE3_EXP, rot_eps=1e-10, trans_eps=1e-10))
     rot_gt, tr_gt = synth.pose_error(r3["T"], fp.T_gt)
     assert rot_gt < np.radians(0.05) and tr_gt < 0.001, (np.degrees(rot_gt), tr_gt)
+
+
+def test_autotune_and_every_launch_shape_give_identical_results(ctx, N, synth):
+    """the autotuner returns a valid launch shape, and the shape never changes a bit
+    of the result (partials are per 1024-point item and summed in item order)"""
+    pairs = synth.batch_pairs(8, seed=3, n_min=20_000, n_max=60_000)
+    srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
+    tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
+    prm = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=True)
+    best, ms = N.icp_autotune(ctx, srcs, tgts, prm, reps=1)
+    assert best.nn_item_points in (64, 128, 256, 512)
+    assert best.nn_blocks_per_sm > 0 and best.accum_blocks_per_sm > 0 and ms > 0
+    ref = N.IcpPlan(ctx, srcs, tgts, prm).execute(results=True)
+    for tune in (best, N.Tuning(64, 4, 2), N.Tuning(512, 20, 12)):
+        p2 = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=True, tuning=tune)
+        got = N.IcpPlan(ctx, srcs, tgts, p2).execute(results=True)
+        for a, b in zip(ref, got):
+            np.testing.assert_array_equal(a["T"], b["T"])
+            assert a["iterations"] == b["iterations"]
