@@ -127,6 +127,9 @@ _SIGS = {
     "gca3d_radius_outlier_removal": [_P, _P, _F, C.c_int, _P],
     "gca3d_cloud_select": [_P, _P, _P, _I64, _P],
     "gca3d_cloud_to_aos": [_P, _P, _P, _P],
+    "gca3d_ply_info": [C.c_char_p, C.POINTER(_I64), C.POINTER(C.c_int), C.POINTER(C.c_int)],
+    "gca3d_ply_read": [C.c_char_p, _P, _P, _P, _I64, C.POINTER(_I64)],
+    "gca3d_ply_write": [C.c_char_p, _P, _P, _P, _I64, C.c_int],
     "gca3d_tracker_create": [_P, C.POINTER(TrackerParams), C.POINTER(_P)],
     "gca3d_tracker_destroy": [_P],
     "gca3d_tracker_frame_buffers": [_P, C.POINTER(_P), C.POINTER(_P)],
@@ -489,3 +492,30 @@ class Tracker:
                 self.ctx.L.gca3d_tracker_destroy(self.h)
         except Exception:
             pass
+
+
+def ply_read(path):
+    """(xyz, rgb or None, normals or None) from a PLY file (host only)"""
+    L = load()
+    n, hn, hc = C.c_int64(), C.c_int(), C.c_int()
+    st = L.gca3d_ply_info(str(path).encode(), C.byref(n), C.byref(hn), C.byref(hc))
+    if st != OK:
+        raise GcaError(st, f"ply_info {path}")
+    xyz = np.empty((n.value, 3), np.float32)
+    rgb = np.empty((n.value, 3), np.float32) if hc.value else None
+    nrm = np.empty((n.value, 3), np.float32) if hn.value else None
+    got = C.c_int64()
+    st = L.gca3d_ply_read(str(path).encode(), _ptr(xyz), _ptr(rgb), _ptr(nrm), n.value, C.byref(got))
+    if st != OK:
+        raise GcaError(st, f"ply_read {path}")
+    return xyz, rgb, nrm
+
+
+def ply_write(path, xyz, rgb=None, nrm=None, binary=True):
+    L = load()
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    rgb = None if rgb is None else np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+    nrm = None if nrm is None else np.ascontiguousarray(nrm, np.float32).reshape(-1, 3)
+    st = L.gca3d_ply_write(str(path).encode(), _ptr(xyz), _ptr(rgb), _ptr(nrm), len(xyz), int(binary))
+    if st != OK:
+        raise GcaError(st, f"ply_write {path}")

@@ -311,6 +311,18 @@ int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *src,
                        gca3d_tuning *best, double *best_ms);
 
 /* ---------------------------------------------------------------------------
+ * PLY point files (host only; no context).  ascii or binary little-endian, a
+ * vertex element with x, y, z and optional nx, ny, nz and red, green, blue (8-bit
+ * colours are scaled by 1/255 as point_cloud::create_from_pcl does,
+ * src/geometry/point_cloud.cu:481-504).  rgb / nrm may be NULL; arrays are n x 3.
+ * ------------------------------------------------------------------------- */
+int gca3d_ply_info(const char *path, int64_t *n_points, int *has_normals, int *has_colors);
+int gca3d_ply_read(const char *path, float *xyz, float *rgb, float *nrm, int64_t cap, int64_t *n);
+/* colours are written as 8-bit (round(c * 255)) */
+int gca3d_ply_write(const char *path, const float *xyz, const float *rgb, const float *nrm, int64_t n,
+                    int binary);
+
+/* ---------------------------------------------------------------------------
  * frame-to-frame tracking of an RGB-D stream (the reference's demo loop,
  * app.cpp:316-350, without its model accumulation)
  * ------------------------------------------------------------------------- */
