@@ -72,6 +72,14 @@ class TrackerParams(C.Structure):
                 ("filter", Filter), ("icp", IcpParams), ("constant_velocity", C.c_int)]
 
 
+class ModelParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("depth_intrin", Intrinsics), ("color_intrin", Intrinsics),
+                ("depth_to_color", Extrinsics), ("depth_scale", C.c_float), ("tmin", C.c_float), ("tmax", C.c_float),
+                ("filter", Filter), ("voxel", C.c_float), ("ror_radius", C.c_float), ("ror_min_neighbors", C.c_int),
+                ("normal_radius", C.c_float), ("max_iter", C.c_int), ("max_corr", C.c_float),
+                ("grad_radius", C.c_float), ("revoxel_every", C.c_int), ("model_capacity", C.c_int64)]
+
+
 class VjpParams(C.Structure):
     _fields_ = [("K", C.c_int), ("max_corr", C.c_float), ("lambda_", C.c_float), ("update_map", C.c_int)]
 
@@ -130,6 +138,10 @@ _SIGS = {
     "gca3d_ply_info": [C.c_char_p, C.POINTER(_I64), C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "gca3d_ply_read": [C.c_char_p, _P, _P, _P, _I64, C.POINTER(_I64)],
     "gca3d_ply_write": [C.c_char_p, _P, _P, _P, _I64, C.c_int],
+    "gca3d_model_create": [_P, C.POINTER(ModelParams), C.POINTER(_P)],
+    "gca3d_model_destroy": [_P],
+    "gca3d_model_push": [_P, _P, _P, C.POINTER(IcpResult), C.POINTER(C.c_int)],
+    "gca3d_model_cloud": [_P, C.POINTER(_P)],
     "gca3d_tracker_create": [_P, C.POINTER(TrackerParams), C.POINTER(_P)],
     "gca3d_tracker_destroy": [_P],
     "gca3d_tracker_frame_buffers": [_P, C.POINTER(_P), C.POINTER(_P)],
@@ -519,3 +531,65 @@ def ply_write(path, xyz, rgb=None, nrm=None, binary=True):
     st = L.gca3d_ply_write(str(path).encode(), _ptr(xyz), _ptr(rgb), _ptr(nrm), len(xyz), int(binary))
     if st != OK:
         raise GcaError(st, f"ply_write {path}")
+
+
+def model_params(cam, tmin=0.2, tmax=2.5, voxel=0.008, ror_radius=0.01, ror_min_neighbors=4, normal_radius=0.04,
+                 max_iter=10, max_corr=0.05, grad_radius=0.05, revoxel_every=5, model_capacity=None,
+                 filter=(FILTER_ADAPTIVE, 0, 0.0, 0.0), depth_scale=0.001):
+    """the reference demo's reconstruction settings (apps/app.cpp:91, 121-128, 315-349)"""
+    p = ModelParams()
+    p.width, p.height = cam.width, cam.height
+    p.depth_intrin = Intrinsics(cam.fx, cam.fy, cam.cx, cam.cy)
+    p.color_intrin = Intrinsics(cam.fx, cam.fy, cam.cx, cam.cy)
+    p.depth_to_color = Extrinsics((C.c_float * 9)(1, 0, 0, 0, 1, 0, 0, 0, 1), (C.c_float * 3)(0, 0, 0))
+    p.depth_scale, p.tmin, p.tmax = depth_scale, tmin, tmax
+    p.filter = Filter(*filter)
+    p.voxel, p.ror_radius, p.ror_min_neighbors = voxel, ror_radius, ror_min_neighbors
+    p.normal_radius, p.max_iter, p.max_corr, p.grad_radius = normal_radius, max_iter, max_corr, grad_radius
+    p.revoxel_every = revoxel_every
+    p.model_capacity = model_capacity or 16 * cam.width * cam.height
+    return p
+
+
+class CloudView(Cloud):
+    """a cloud owned by another object (no destroy)"""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.h = handle
+        c = C.c_int64()
+        ctx.check(ctx.L.gca3d_cloud_capacity(handle, C.byref(c)))
+        self.capacity = c.value
+
+    def __del__(self):
+        pass
+
+
+class Model:
+    """the frame-to-model accumulation loop of the reference demo"""
+
+    def __init__(self, ctx, params):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        ctx.check(ctx.L.gca3d_model_create(ctx.h, C.byref(params), C.byref(self.h)))
+        self._res = IcpResult()
+
+    def push(self, depth, bgr):
+        """returns (registration result dict, appended)"""
+        d = np.ascontiguousarray(depth, np.uint16)
+        c = np.ascontiguousarray(bgr, np.uint8)
+        app = C.c_int()
+        self.ctx.check(self.ctx.L.gca3d_model_push(self.h, _ptr(d), _ptr(c), C.byref(self._res), C.byref(app)))
+        return result_dict(self._res), bool(app.value)
+
+    def cloud(self):
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.L.gca3d_model_cloud(self.h, C.byref(h)))
+        return CloudView(self.ctx, h)
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.L.gca3d_model_destroy(self.h)
+        except Exception:
+            pass

@@ -356,6 +356,44 @@ int gca3d_tracker_push(gca3d_tracker *tracker, const uint16_t *depth, const uint
 int gca3d_tracker_kernels(gca3d_tracker *tracker, int64_t *n);
 
 /* ---------------------------------------------------------------------------
+ * frame-to-model accumulation (the reference demo's reconstruction loop,
+ * apps/app.cpp:111-128 and 315-349).  The model lives in the latest camera's
+ * coordinates.  Reference settings: voxel 0.008, ror_radius 0.01,
+ * ror_min_neighbors 4, normal_radius 0.04, max_iter 10, max_corr 0.05,
+ * grad_radius 0.05, revoxel_every 5, filter mode GCA3D_FILTER_ADAPTIVE, t_min 0.2,
+ * t_max 2.5.
+ * ------------------------------------------------------------------------- */
+typedef struct gca3d_model gca3d_model;
+typedef struct gca3d_model_params {
+    int width, height;
+    gca3d_intrinsics depth_intrin;
+    gca3d_intrinsics color_intrin;
+    gca3d_extrinsics depth_to_color;
+    float depth_scale, tmin, tmax;
+    gca3d_filter filter;
+    float voxel;            /* frame and model downsampling */
+    float ror_radius;       /* radius outlier removal of each frame */
+    int ror_min_neighbors;
+    float normal_radius;
+    int max_iter;           /* colored ICP of the model (or previous frame) onto the frame */
+    float max_corr;
+    float grad_radius;
+    int revoxel_every;      /* re-voxelise the model after this many appends */
+    int64_t model_capacity; /* points; at least width * height */
+} gca3d_model_params;
+
+int gca3d_model_create(gca3d_context *ctx, const gca3d_model_params *params, gca3d_model **model);
+int gca3d_model_destroy(gca3d_model *model);
+/* one frame (host or device pointers).  result (may be NULL): the registration onto this
+ * frame (status GCA3D_ERR_NO_CORRESPONDENCES for the first frame); appended (may be
+ * NULL): 1 when the frame was added to the model.  A model that outgrows its capacity
+ * gives GCA3D_ERR_CAPACITY. */
+int gca3d_model_push(gca3d_model *model, const uint16_t *depth, const uint8_t *bgr,
+                     gca3d_icp_result *result, int *appended);
+/* the model cloud (owned by the model object; valid until the next push) */
+int gca3d_model_cloud(gca3d_model *model, gca3d_cloud **cloud);
+
+/* ---------------------------------------------------------------------------
  * adjoint of K unrolled Gauss-Newton steps (no reference counterpart)
  * ------------------------------------------------------------------------- */
 #define GCA3D_VJP_MAX_STEPS 64
