@@ -9,7 +9,7 @@
 // device and compacts with thrust::remove_if.  Here a block owns one image row:
 // it stages the 2R+1 depth rows around it in shared memory, filters and
 // back-projects its pixels, ranks the valid ones in raster order with block scans,
-// takes the row's output offset from the rows above by decoupled look-back (bounded
+// takes the row's output offset from the rows above by a warp-wide decoupled look-back (bounded
 // spin) and writes the compacted SoA points directly.  Same arithmetic order as the
 // reference (unfused multiply/add); the filter weights use det_expf below instead
 // of expf, so the CPU oracle reproduces every output bit.
@@ -187,45 +187,62 @@ __global__ void __launch_bounds__(kFrameThreads) k_frame(const uint16_t *__restr
         row_count += total;
         __syncthreads();
     }
-    // decoupled look-back over rows
-    if (threadIdx.x == 0)
+    // decoupled look-back over rows, one warp: the 32 nearest predecessors' states are
+    // read at once (each wait bounded), the nearest inclusive prefix is found by ballot
+    // and the aggregates up to it are summed by the warp; only a window without an
+    // inclusive state moves the look-back 32 rows further up
+    if (warp == 0)
     {
-        long long excl = 0;
         unsigned long long *st = status + y;
-        if (y == 0)
-            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(kRowInc | (unsigned long long)row_count)
-                         : "memory");
-        else
+        long long excl = 0;
+        if (lane == 0)
         {
-            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(kRowAgg | (unsigned long long)row_count)
-                         : "memory");
-            for (int p = y - 1; p >= 0; --p)
+            const unsigned long long v = (y == 0 ? kRowInc : kRowAgg) | (unsigned long long)row_count;
+            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st), "l"(v) : "memory");
+        }
+        if (y > 0)
+        {
+            for (int top = y - 1;; top -= 32)
             {
-                unsigned long long s;
-                unsigned spins = 0;
-                asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(s) : "l"(status + p) : "memory");
-                while ((s & kRowFlag) == 0)
+                const int p = top - lane;
+                unsigned long long s = kRowInc; // above row 0: an inclusive zero
+                if (p >= 0)
                 {
-                    if (++spins > kSpinLimit)
-                    {
-                        atomicOr(d_err, kErrTimeout);
-                        break;
-                    }
-                    if (spins > 64)
-                        __nanosleep(64);
+                    unsigned spins = 0;
                     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(s) : "l"(status + p) : "memory");
+                    while ((s & kRowFlag) == 0)
+                    {
+                        if (++spins > kSpinLimit)
+                        {
+                            atomicOr(d_err, kErrTimeout);
+                            break; // a state that never came counts as the end of the look-back
+                        }
+                        if (spins > 64)
+                            __nanosleep(64);
+                        asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(s) : "l"(status + p) : "memory");
+                    }
                 }
-                excl += (long long)(s & ~kRowFlag);
-                if ((s & kRowFlag) != kRowAgg)
+                const unsigned inc = __ballot_sync(0xffffffffu, (s & kRowFlag) != kRowAgg);
+                const int stop = inc ? __ffs(inc) - 1 : 31;
+                long long v = lane <= stop ? (long long)(s & ~kRowFlag) : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                excl += v;
+                if (inc)
                     break;
             }
-            asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st),
-                         "l"(kRowInc | (unsigned long long)(excl + row_count))
-                         : "memory");
+            if (lane == 0)
+                asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(st),
+                             "l"(kRowInc | (unsigned long long)(excl + row_count))
+                             : "memory");
         }
-        s_base = excl;
-        if (y == P.h - 1)
-            *d_count = (int32_t)(excl + row_count);
+        if (lane == 0)
+        {
+            s_base = excl;
+            if (y == P.h - 1)
+                *d_count = (int32_t)(excl + row_count);
+        }
     }
     __syncthreads();
     const long long base = s_base;

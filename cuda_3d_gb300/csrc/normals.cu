@@ -255,13 +255,18 @@ __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n
             syy += dy * dy, syz += dy * dz, szz += dz * dz;
             ++k;
         };
-        if (inside && max_nn <= 0)
+        // every neighbour inside the radius; only when there are more than max_nn
+        // are the max_nn nearest selected instead (most points have fewer, and then
+        // the two sets are the same)
+        if (inside)
             grid_scan(g, R, [&](int t, float4 q) {
                 if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
                     acc(q);
             });
-        else if (inside)
+        if (inside && max_nn > 0 && k > max_nn)
         {
+            s1x = s1y = s1z = sxx = sxy = sxz = syy = syz = szz = 0.0f;
+            k = 0;
             const int cnt = select_knn(g, R, p, rn2, max_nn, list);
             for (int j = 0; j < cnt; ++j)
                 acc(g.spos[list[j].t]);
@@ -311,13 +316,16 @@ __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_
             S2[3] += dy * dy, S2[4] += dy * dz, S2[5] += dz * dz;
             ++k;
         };
-        if (max_nn <= 0)
-            grid_scan(g, R, [&](int t, float4 q) {
-                if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
-                    acc(q);
-            });
-        else
+        grid_scan(g, R, [&](int t, float4 q) {
+            if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                acc(q);
+        });
+        if (max_nn > 0 && k > max_nn)
         {
+            S1[0] = S1[1] = S1[2] = 0.0;
+            for (int i = 0; i < 6; ++i)
+                S2[i] = 0.0;
+            k = 0;
             const int cnt = select_knn(g, R, p, rn2, max_nn, list);
             for (int i = 0; i < cnt; ++i)
                 acc(g.spos[list[i].t]);

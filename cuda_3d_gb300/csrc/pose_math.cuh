@@ -10,99 +10,157 @@ namespace gca3d
 // ---------------------------------------------------------------------------
 // FP64 6x6 solve and pose maps (device; the oracle restates the same steps)
 // ---------------------------------------------------------------------------
+// exact selects on the bit patterns: a conditional written with ?: over a set of
+// static indices is turned back into a runtime index by the compiler, which moves
+// the array to local memory
+__device__ __forceinline__ double bsel(bool s, double a, double b)
+{
+    const long long m = -(long long)s;
+    return __longlong_as_double((__double_as_longlong(a) & m) | (__double_as_longlong(b) & ~m));
+}
+__device__ __forceinline__ int isel(bool s, int a, int b)
+{
+    const int m = -(int)s;
+    return (a & m) | (b & ~m);
+}
+
+// Every loop is unrolled and every array index is a compile-time constant: the
+// pivot's row / column exchange is a conditional swap (bsel) against each candidate
+// row, so the matrix stays in registers (the solve is one thread's dependent FP64
+// chain on the ICP critical path; in local memory it cost several times more).
 __device__ inline int solve6_device(const double *S /* 21 upper + 6 rhs */, double x[6])
 {
+    constexpr double kTiny = 2.2250738585072014e-308;
     double A[6][6], b[6], D[6];
     int perm[6];
     int status = 0;
-    int u = 0;
-    for (int i = 0; i < 6; ++i)
-        for (int j = i; j < 6; ++j)
-        {
-            A[i][j] = A[j][i] = S[u];
-            ++u;
-        }
+    {
+        int u = 0;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = i; j < 6; ++j)
+            {
+                A[i][j] = A[j][i] = S[u];
+                ++u;
+            }
+    }
+#pragma unroll
     for (int i = 0; i < 6; ++i)
     {
         b[i] = -S[21 + i];
         perm[i] = i;
-    }
-    for (int i = 0; i < 6; ++i)
-    {
         if (!isfinite(b[i]))
             status = 1;
+#pragma unroll
         for (int j = 0; j < 6; ++j)
             if (!isfinite(A[i][j]))
                 status = 1;
     }
     if (status)
     {
+#pragma unroll
         for (int i = 0; i < 6; ++i)
             x[i] = 0.0;
         return 1;
     }
+#pragma unroll
     for (int k = 0; k < 6; ++k)
     {
+        // symmetric pivot: the largest remaining diagonal entry (first one on ties)
         int piv = k;
+        double best = fabs(A[k][k]);
+#pragma unroll
         for (int i = k + 1; i < 6; ++i)
-            if (fabs(A[i][i]) > fabs(A[piv][piv]))
-                piv = i;
-        if (piv != k)
         {
+            const double v = fabs(A[i][i]);
+            if (v > best)
+            {
+                best = v;
+                piv = i;
+            }
+        }
+#pragma unroll
+        for (int i = k + 1; i < 6; ++i)
+        {
+            const bool sw = piv == i;
+#pragma unroll
             for (int j = 0; j < 6; ++j)
             {
-                double t = A[k][j];
-                A[k][j] = A[piv][j];
-                A[piv][j] = t;
+                const double t = A[k][j];
+                A[k][j] = bsel(sw, A[i][j], t);
+                A[i][j] = bsel(sw, t, A[i][j]);
             }
-            for (int i = 0; i < 6; ++i)
+#pragma unroll
+            for (int j = 0; j < 6; ++j)
             {
-                double t = A[i][k];
-                A[i][k] = A[i][piv];
-                A[i][piv] = t;
+                const double t = A[j][k];
+                A[j][k] = bsel(sw, A[j][i], t);
+                A[j][i] = bsel(sw, t, A[j][i]);
             }
-            int t = perm[k];
-            perm[k] = perm[piv];
-            perm[piv] = t;
+            const int tp = perm[k];
+            perm[k] = isel(sw, perm[i], tp);
+            perm[i] = isel(sw, tp, perm[i]);
         }
         D[k] = A[k][k];
-        if (fabs(D[k]) <= 2.2250738585072014e-308)
+        if (fabs(D[k]) <= kTiny)
         {
             status = 1;
+#pragma unroll
             for (int i = k + 1; i < 6; ++i)
                 A[i][k] = 0.0;
-            continue;
         }
-        // one reciprocal per pivot: FP64 division is a long dependent sequence here
-        const double inv = 1.0 / D[k];
-        for (int i = k + 1; i < 6; ++i)
-            A[i][k] *= inv;
-        for (int i = k + 1; i < 6; ++i)
-            for (int j = k + 1; j <= i; ++j)
-            {
-                A[i][j] -= A[i][k] * A[j][k] * D[k];
-                A[j][i] = A[i][j];
-            }
+        else
+        {
+            // one reciprocal per pivot: FP64 division is a long dependent sequence
+            const double inv = 1.0 / D[k];
+#pragma unroll
+            for (int i = k + 1; i < 6; ++i)
+                A[i][k] *= inv;
+#pragma unroll
+            for (int i = k + 1; i < 6; ++i)
+#pragma unroll
+                for (int j = k + 1; j <= i; ++j)
+                {
+                    A[i][j] -= A[i][k] * A[j][k] * D[k];
+                    A[j][i] = A[i][j];
+                }
+        }
     }
     double y[6], z[6];
+#pragma unroll
     for (int i = 0; i < 6; ++i)
     {
-        double s = b[perm[i]];
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < 6; ++q)
+            s = bsel(perm[i] == q, b[q], s);
+#pragma unroll
         for (int j = 0; j < i; ++j)
             s -= A[i][j] * y[j];
         y[i] = s;
     }
+#pragma unroll
     for (int i = 0; i < 6; ++i)
-        y[i] = fabs(D[i]) > 2.2250738585072014e-308 ? y[i] / D[i] : 0.0;
+        y[i] = fabs(D[i]) > kTiny ? y[i] / D[i] : 0.0;
+#pragma unroll
     for (int i = 5; i >= 0; --i)
     {
         double s = y[i];
+#pragma unroll
         for (int j = i + 1; j < 6; ++j)
             s -= A[j][i] * z[j];
         z[i] = s;
     }
-    for (int i = 0; i < 6; ++i)
-        x[perm[i]] = z[i];
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+    {
+        double v = 0.0;
+#pragma unroll
+        for (int i = 0; i < 6; ++i)
+            v = bsel(perm[i] == q, z[i], v);
+        x[q] = v;
+    }
     return status;
 }
 
