@@ -274,6 +274,140 @@ __device__ __forceinline__ NNBest nn_search_box(const GridDev &g, const KeyLayou
     return b;
 }
 
+// ---------------------------------------------------------------------------
+// Correspondence certificates.  A search at position ps also yields a lower bound
+// G on the distance from ps to every target point other than the nearest one t1:
+// the second-smallest squared distance it saw, and the radius of the ball that the
+// searched cells contain (points outside were not seen).  While the source point
+// moves by delta from ps, no other point can come closer than G - delta, so a
+// fresh distance to t1 below that proves t1 is still the unique nearest point.
+// Every FP32 rounding on the way is covered by relative slack of a few 1e-6
+// (distances are computed to within 6 units of 2^-24).
+// ---------------------------------------------------------------------------
+struct NNCerts
+{
+    float4 *pos; // ps (the transformed source point of the last search), w = G
+    int *t;      // t1: the nearest point that search found at any distance, -1 for none
+};
+
+struct NNBest2
+{
+    float d2; // nearest (any distance), +inf when the searched cells are empty
+    int t;
+    float s2; // second-smallest squared distance, +inf when fewer than two points
+};
+
+// radius R of the ball around p whose points all lie in cells of box B: each
+// axis's bound is checked through cell_of itself, with p - R rounded down and
+// p + R rounded up (cell_of is monotonic, and it is how the grid binned its
+// points).  0 when no positive radius passes.
+__device__ __forceinline__ float box_cover(const GridDev &g, float3 o, float3 p, const CellBox &B)
+{
+    const float c = g.cell;
+    const float fx0 = o.x + (float)B.x0 * c, fx1 = o.x + (float)(B.x0 + B.nx) * c;
+    const float fy0 = o.y + (float)B.y0 * c, fy1 = o.y + (float)(B.y0 + B.ny) * c;
+    const float fz0 = o.z + (float)B.zlo * c, fz1 = o.z + (float)(B.zhi + 1) * c;
+    float r = fminf(fminf(fminf(p.x - fx0, fx1 - p.x), fminf(p.y - fy0, fy1 - p.y)), fminf(p.z - fz0, fz1 - p.z));
+    r = r * 0.99998f - 1e-6f * (1.0f + fmaxf(fmaxf(fabsf(p.x), fabsf(p.y)), fabsf(p.z)));
+    if (!(r > 0.0f))
+        return 0.0f;
+    const bool ok = cell_of(__fsub_rd(p.x, r), o.x, c) >= B.x0 && cell_of(__fadd_ru(p.x, r), o.x, c) < B.x0 + B.nx &&
+                    cell_of(__fsub_rd(p.y, r), o.y, c) >= B.y0 && cell_of(__fadd_ru(p.y, r), o.y, c) < B.y0 + B.ny &&
+                    cell_of(__fsub_rd(p.z, r), o.z, c) >= B.zlo && cell_of(__fadd_ru(p.z, r), o.z, c) <= B.zhi;
+    return ok ? r : 0.0f;
+}
+
+// the nearest grid point inside box B at any distance (ties to the smaller original
+// index, as nn_search_box) and the second-smallest squared distance, over the
+// 4-lane group; all 32 lanes of the warp call it
+__device__ __forceinline__ NNBest2 nn_search_box2(const GridDev &g, const KeyLayout &L, int seg, const CellBox &B,
+                                                  float3 p, bool valid)
+{
+    const int sub = threadIdx.x & (kSub - 1);
+    NNBest2 b{INFINITY, -1, INFINITY};
+    SubRows R;
+    if (valid)
+    {
+        grid_rows_box(g, L, seg, B, sub, R);
+        grid_scan_sub(g, R, [&](int t, float4 q) {
+            const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+            if (b.t < 0 || d2 < b.d2 || (d2 == b.d2 && __ldg(&g.sidx[t]) < __ldg(&g.sidx[b.t])))
+            {
+                b.s2 = b.d2;
+                b.d2 = d2;
+                b.t = t;
+            }
+            else
+                b.s2 = fminf(b.s2, d2);
+        });
+    }
+#pragma unroll
+    for (int off = 1; off < kSub; off <<= 1)
+    {
+        const float od2 = __shfl_xor_sync(0xffffffffu, b.d2, off, kSub);
+        const int ot = __shfl_xor_sync(0xffffffffu, b.t, off, kSub);
+        const float os2 = __shfl_xor_sync(0xffffffffu, b.s2, off, kSub);
+        if (ot >= 0 && (b.t < 0 || od2 < b.d2 || (od2 == b.d2 && __ldg(&g.sidx[ot]) < __ldg(&g.sidx[b.t]))))
+        {
+            b.s2 = fminf(os2, b.d2);
+            b.d2 = od2;
+            b.t = ot;
+        }
+        else
+            b.s2 = fminf(b.s2, od2);
+    }
+    return b;
+}
+
+// G of a search at p over box B (see NNCerts)
+__device__ __forceinline__ float cert_bound(const GridDev &g, float3 o, float3 p, const CellBox &B, float s2)
+{
+    float G = box_cover(g, o, p, B);
+    if (s2 < INFINITY)
+        G = fminf(G, sqrtf(s2) * 0.999998f);
+    return G;
+}
+
+// the correspondence of p from a certificate (ps, G, t1), without a search; false
+// when the certificate does not decide it.  On true, t is what the search over the
+// 27 cells around p gives (nearest with d^2 < rr, ties to the smaller index, -1 for
+// none) and d2 its squared distance.
+__device__ __forceinline__ bool nn_certified(const GridDev &g, float3 o, float3 p, const CellBox &B, float4 cp,
+                                             int t1, float rr, int &t, float &d2)
+{
+    const float dx = p.x - cp.x, dy = p.y - cp.y, dz = p.z - cp.z;
+    const float delta = sqrtf(dx * dx + dy * dy + dz * dz) * 1.000002f;
+    const float m = cp.w - delta; // every other point is at least this far from p
+    if (!(m > 1e-6f))
+        return false;
+    const float m2 = m * m * 0.999996f; // below the FP32 squared distance of every other point
+    if (t1 < 0)
+    {
+        if (!(m2 >= rr * 1.000001f))
+            return false;
+        t = -1;
+        d2 = rr;
+        return true;
+    }
+    const float4 q = __ldg(&g.spos[t1]);
+    const float dq = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+    if (!(dq < m2))
+        return false;
+    d2 = dq;
+    if (!(dq < rr))
+    {
+        t = -1; // t1 is the nearest and it is beyond max_corr
+        d2 = rr;
+        return true;
+    }
+    // t1 must also be one of the candidates of the 27-cell search around p
+    const int qx = cell_of(q.x, o.x, g.cell), qy = cell_of(q.y, o.y, g.cell), qz = __float_as_int(q.w);
+    if (qx < B.x0 || qx >= B.x0 + B.nx || qy < B.y0 || qy >= B.y0 + B.ny || qz < B.zlo || qz > B.zhi)
+        return false;
+    t = t1;
+    return true;
+}
+
 // the nearest grid point with d^2 < rr in the 27 cells around p (4-lane group)
 __device__ __forceinline__ NNBest nn_search_sub(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p,
                                                 float rr, bool valid)

@@ -9,7 +9,8 @@
 // of one pair's source points.  k_icp_nn transforms them by the pair's current pose
 // and finds the nearest target point inside max_corr (row-hashed grid, ties to the
 // smaller index); it keeps few registers so many warps hide the latency of the
-// neighbour walk.  k_icp_accum builds the geometric and photometric residuals and
+// neighbour walk, and it skips the walk for points whose certificate from an
+// earlier search of the scale still decides the answer (grid_query.cuh).  k_icp_accum builds the geometric and photometric residuals and
 // their 6-vector Jacobians in FP32 and accumulates the 21 + 6 + 1 system terms plus
 // the correspondence count and squared distances.  Accumulation is compensated
 // FP32 inside the block (two-sum per thread and per shuffle level) and FP64 across
@@ -238,39 +239,78 @@ __device__ __forceinline__ BlockPair item_pair(int w, const int32_t *src_off, co
 }
 
 // step 1 of an iteration: the correspondence of every active source point
-// (grid position and squared distance, -1 when none within max_corr).  From the
-// second iteration of a scale on, the point's previous correspondence (same grid)
-// is a candidate at a known distance u: the search shrinks to the cells that
-// overlap the ball of radius u, which holds the nearest point and all its ties.
+// (grid position and squared distance, -1 when none within max_corr).
+// Phase 1, one thread per point: from the second iteration of a scale on, a point
+// whose certificate from its last search still holds (it has not moved far enough
+// for another target point to overtake its nearest one, grid_query.cuh) takes its
+// correspondence without a search.  Phase 2, four lanes per point over the block's
+// list of the others: the search, shrunk to the cells that overlap the ball
+// through the last nearest point when that one is within max_corr (the ball holds
+// the nearest point and all its ties); it renews the point's certificate.
 __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                         GridDev g, const PairState *st, const int *bmap, int P,
-                                                        float max_corr, int2 *corr, const int2 *corr_prev,
-                                                        int32_t *nn_out, int nn_chunk)
+                                                        float max_corr, int2 *corr, NNCerts cert, int32_t *nn_out,
+                                                        int nn_chunk)
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
+    __shared__ int s_list[kNNChunkMax];
+    __shared__ int s_cnt;
     const KeyLayout L = *g.layout;
     const float rr = __fmul_rn(max_corr, max_corr);
     const int items = bmap[P];
+    const int lane = threadIdx.x & 31;
     for (int w = blockIdx.x; w < items; w += gridDim.x)
     {
     const BlockPair b = item_pair(w, src_off, st, bmap, P, nn_chunk, s_T, &s_pair);
     if (b.pair < 0)
         continue;
+    if (threadIdx.x == 0)
+        s_cnt = 0;
+    __syncthreads();
     const float3 o = g.gmin[b.pair];
     const int tbase = g.seg_off[b.pair];
-    const bool warm = corr_prev && st[b.pair].nn_warm;
-    // four lanes per source point (uniform trip count for the whole block)
-    for (int base = b.start; base < b.end; base += kIcpThreads / kSub)
+    const bool warm = st[b.pair].nn_warm;
+    for (int base = b.start; base < b.end; base += kIcpThreads)
     {
-        const int i = base + (int)(threadIdx.x / kSub);
-        const bool valid = i < b.end;
-        const float3 p = apply_pose(s_T, src_pos[valid ? i : b.start]);
+        const int i = base + (int)threadIdx.x;
+        bool need = i < b.end;
+        if (need && warm)
+        {
+            const float3 p = apply_pose(s_T, src_pos[i]);
+            CellBox B;
+            int t;
+            float d2;
+            if (nn_full_box(g, L, o, p, B) && nn_certified(g, o, p, B, cert.pos[i], cert.t[i], rr, t, d2))
+            {
+                need = false;
+                corr[i] = make_int2(t, __float_as_int(d2));
+                if (nn_out)
+                    nn_out[i] = t >= 0 ? __ldg(&g.sidx[t]) - tbase : -1;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, need);
+        int at = 0;
+        if (lane == 0 && m)
+            at = atomicAdd(&s_cnt, __popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (need)
+            s_list[at + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+    __syncthreads();
+    const int n = s_cnt;
+    // four lanes per listed point (uniform trip count for the whole block)
+    for (int base = 0; base < n; base += kIcpThreads / kSub)
+    {
+        const int k = base + (int)(threadIdx.x / kSub);
+        const bool valid = k < n;
+        const int i = s_list[valid ? k : 0];
+        const float3 p = apply_pose(s_T, src_pos[i]);
         CellBox B;
         const bool in = nn_full_box(g, L, o, p, B);
         if (warm && valid && in)
         {
-            const int t = corr_prev[i].x;
+            const int t = cert.t[i];
             if (t >= 0)
             {
                 const float4 q = __ldg(&g.spos[t]);
@@ -279,12 +319,15 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
                     nn_shrink_box(g, o, p, sqrtf(d2), B);
             }
         }
-        const NNBest best = nn_search_box(g, L, b.pair, B, p, rr, valid && in);
+        const NNBest2 best = nn_search_box2(g, L, b.pair, B, p, valid && in);
         if (valid && (threadIdx.x & (kSub - 1)) == 0)
         {
-            corr[i] = make_int2(best.t, __float_as_int(best.d2));
+            const bool hit = best.t >= 0 && best.d2 < rr;
+            corr[i] = make_int2(hit ? best.t : -1, __float_as_int(hit ? best.d2 : rr));
             if (nn_out)
-                nn_out[i] = best.t >= 0 ? __ldg(&g.sidx[best.t]) - tbase : -1;
+                nn_out[i] = hit ? __ldg(&g.sidx[best.t]) - tbase : -1;
+            cert.pos[i] = make_float4(p.x, p.y, p.z, in ? cert_bound(g, o, p, B, best.s2) : 0.0f);
+            cert.t[i] = best.t;
         }
     }
     }
@@ -512,7 +555,7 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
 
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
-                  int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated, int32_t *nn_out,
+                  int2 *corr, const NNCerts &cert, const IcpScale &prm, bool compensated, int32_t *nn_out,
                   const IcpLoop &loop, const IcpShape &shape)
 {
     if (!loop.ticket)
@@ -523,7 +566,7 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
     const int grid_acc = std::max(std::min(max_blocks, ctx->num_sms * shape.acc_bps), 1);
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
     k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
-                                                       corr, corr_prev, nn_out, shape.nn_chunk);
+                                                       corr, cert, nn_out, shape.nn_chunk);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
         k_icp_accum<true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,

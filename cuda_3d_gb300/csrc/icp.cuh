@@ -1,6 +1,7 @@
 // icp.cuh -- per-pair device state and per-scale parameters of the ICP kernels.
 #pragma once
 
+#include "grid_query.cuh"
 #include "stages.cuh"
 
 namespace gca3d
@@ -10,6 +11,7 @@ constexpr int kIcpThreads = 256;
 constexpr int kIcpChunk = 1024; // source points per accumulate work item (one partial each)
 constexpr int kNNChunk = 256;   // default source points per correspondence work item
 constexpr int kNNChunkMin = 64; // the smallest item size a tuning may choose
+constexpr int kNNChunkMax = 512; // the largest
 
 // the launch shape in force (defaults filled in)
 struct IcpShape
@@ -87,7 +89,7 @@ int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, 
               int *bmap_nn, int scale, int nn_chunk);
 int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
                   PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
-                  int2 *corr, const int2 *corr_prev, const IcpScale &prm, bool compensated, int32_t *nn_out,
+                  int2 *corr, const NNCerts &cert, const IcpScale &prm, bool compensated, int32_t *nn_out,
                   const IcpLoop &loop, const IcpShape &shape);
 int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
              double *out30);

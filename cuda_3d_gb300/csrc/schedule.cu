@@ -133,11 +133,13 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         float4 *attr1 = ctx->arena.get<float4>(g.cap);
         double *partials = ctx->arena.get<double>((size_t)std::max(pl->max_blocks, 1) * kTermsPad);
         int2 *corr = ctx->arena.get<int2>(std::max<int64_t>(bs.cap, 1));
+        const NNCerts cert{ctx->arena.get<float4>(std::max<int64_t>(bs.cap, 1)),
+                           ctx->arena.get<int>(std::max<int64_t>(bs.cap, 1))};
         int *bmap = ctx->arena.get<int>(P + 1);
         int *bmap_nn = ctx->arena.get<int>(P + 1);
         float4 *nrm_b = own_nn_grid && !keep ? ctx->arena.get<float4>(g.cap) : nullptr;
         float4 *grd_b = own_nn_grid ? ctx->arena.get<float4>(g.cap) : nullptr;
-        if (!attr0 || !attr1 || !partials || !corr || !bmap || !bmap_nn || (own_nn_grid && (!grd_b || (!keep && !nrm_b))))
+        if (!attr0 || !attr1 || !partials || !corr || !cert.pos || !cert.t || !bmap || !bmap_nn || (own_nn_grid && (!grd_b || (!keep && !nrm_b))))
             return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
         if (own_nn_grid)
         {
@@ -195,7 +197,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             loop.iter = iter;
             loop.max_iter = S.max_iter;
             st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                               pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr, loop,
+                               pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr, loop,
                                shape);
             pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
             ctx->stream = main_stream;
@@ -211,7 +213,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         for (int it = 0; it < S.max_iter; ++it)
         {
             if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                                    pl->max_blocks_nn, partials, corr, corr, prm, p.compensated != 0, nullptr,
+                                    pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr,
                                     loop, shape)))
                 return st;
             if (pl->host_checks && !capturing)

@@ -300,9 +300,11 @@ extern "C" int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_c
     int *bmap_nn = ctx->arena.get<int>(2);
     double *partials = ctx->arena.get<double>((size_t)max_blocks * kTermsPad);
     int2 *corr = ctx->arena.get<int2>((size_t)(K + 1) * src->capacity);
+    const NNCerts cert{ctx->arena.get<float4>(src->capacity), ctx->arena.get<int>(src->capacity)};
     IcpTrace *trace = ctx->arena.get<IcpTrace>(K + 1);
     unsigned *fticket = ctx->arena.get<unsigned>(1);
-    if (!attr0 || !attr1 || !pst || !bmap || !bmap_nn || !partials || !corr || !trace || !fticket)
+    if (!attr0 || !attr1 || !pst || !bmap || !bmap_nn || !partials || !corr || !cert.pos || !cert.t || !trace ||
+        !fticket)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp vjp: scratch");
     if ((st = gather_attrs(ctx, bt, g, tgt->nrm, tgt->grd, attr0, attr1)))
         return st;
@@ -332,8 +334,7 @@ extern "C" int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_c
     loop.ticket = fticket;
     for (int k = 0; k <= K; ++k)
         if ((st = icp_iteration(ctx, bs, g, attr0, attr1, pst, bmap, max_blocks, bmap_nn, max_blocks_nn, partials,
-                                corr + (size_t)k * src->capacity,
-                                k ? corr + (size_t)(k - 1) * src->capacity : nullptr, prm, true,
+                                corr + (size_t)k * src->capacity, cert, prm, true,
                                 d_corr ? d_corr + (size_t)k * ns : nullptr, loop, shape)))
             return st;
 

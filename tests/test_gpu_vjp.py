@@ -235,3 +235,28 @@ def test_pruned_correspondences_are_exact(ctx, N, orc, c2):
         p = orc.apply_pose_f32(Tk, sx)
         nn = orc.nn_search(p, tx, MAX_CORR, tie=orc.TIE_MIN_INDEX)
         np.testing.assert_array_equal(r["corr"][k], nn)
+
+
+@pytest.mark.parametrize("xi_scale", [0.0, 1.0])
+def test_certified_correspondences_are_exact(ctx, N, orc, c2, xi_scale):
+    """Once a point has been searched, later evaluations of the scale decide its
+    correspondence from a certificate when it has not moved far enough for another
+    target point to overtake its nearest one (or to come within max_corr of an
+    unmatched point).  Over 16 Gauss-Newton steps -- large moves first (from the
+    identity, a 10 degree / 10 cm offset), then converging ones where most points
+    are decided that way -- every evaluation's correspondences must equal an
+    exhaustive search at the same FP32 points."""
+    K = 16
+    pr = c2["pr"]
+    xi0 = xi_scale * c2["xi0"]
+    r = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], xi0, K=K, max_corr=MAX_CORR, want_corr=True)
+    sx = np.asarray(pr.src_xyz, np.float32)
+    tx = np.asarray(pr.tgt_xyz, np.float32)
+    matched = []
+    for k in range(1, K + 1):
+        Tk = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], xi0, K=k, max_corr=MAX_CORR)["T"]
+        p = orc.apply_pose_f32(Tk, sx)
+        nn = orc.nn_search(p, tx, MAX_CORR, tie=orc.TIE_MIN_INDEX)
+        np.testing.assert_array_equal(r["corr"][k], nn, err_msg=f"evaluation {k}")
+        matched.append((nn >= 0).mean())
+    assert matched[-1] > 0.4  # the views overlap: most evaluations match many points
