@@ -69,6 +69,7 @@ __global__ void k_grid_layout(const int *ord, int P, float cell, int mode, float
         L.by = bitlen_u32(s_max[1]);
         L.bz = bitlen_u32(s_max[2]);
         L.total_bits = L.bseg + L.bx + L.by + L.bz;
+        L.morton = 0;
         if (L.total_bits > 64)
             atomicOr(d_err, kErrKeyBits);
         *lay = L;
@@ -166,6 +167,7 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     g.hcap = hcap;
     GridDev &d = g.dev;
     d.cell = cell;
+    d.inv_cell = 1.0f / cell;
     d.gmin = A.get<float3>(P);
     d.layout = A.get<KeyLayout>(1);
     d.spos = A.get<float4>(cap);

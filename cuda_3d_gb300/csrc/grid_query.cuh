@@ -218,21 +218,36 @@ __device__ __forceinline__ bool nn_full_box(const GridDev &g, const KeyLayout &L
     return !(cx < -1 || cx > mx + 1 || cy < -1 || cy > my + 1 || cz < -1 || cz > mz + 1);
 }
 
+// cell bounds without a division: the cell that cell_of assigns to any value v'
+// >= v (resp. <= v) is at least lo_cell(v) (resp. at most hi_cell(v)).  The quotient
+// by the reciprocal is within 3 rounding units of (v - o) / cell and the binning
+// itself (sub, div) within 2, so a slack of 1e-6 (|a| + 3) cells covers both.
+__device__ __forceinline__ int lo_cell(float v, float o, float inv)
+{
+    const float a = (v - o) * inv;
+    return __float2int_rd(a - 1e-6f * (fabsf(a) + 3.0f));
+}
+__device__ __forceinline__ int hi_cell(float v, float o, float inv)
+{
+    const float a = (v - o) * inv;
+    return __float2int_rd(a + 1e-6f * (fabsf(a) + 3.0f));
+}
+
 // shrink a full box to the cells that overlap the ball of radius u around p.  u
 // bounds the distance of the nearest point (a known candidate lies at that
 // distance), so the nearest point -- and every point that could tie with it -- is
 // in the smaller box.  u is inflated for the rounding of the distance and of p -/+ u;
-// cell_of is monotonic, so the cell range of the ball contains the cells of all its
-// points.
+// lo_cell / hi_cell bound the cells of every point of the ball.
 __device__ __forceinline__ void nn_shrink_box(const GridDev &g, float3 o, float3 p, float u, CellBox &B)
 {
     const float ui = u * 1.00002f + 1e-6f * (1.0f + fabsf(p.x) + fabsf(p.y) + fabsf(p.z));
-    const int x0 = max(cell_of(__fsub_rn(p.x, ui), o.x, g.cell), B.x0);
-    const int x1 = min(cell_of(__fadd_rn(p.x, ui), o.x, g.cell), B.x0 + 2);
-    const int y0 = max(cell_of(__fsub_rn(p.y, ui), o.y, g.cell), B.y0);
-    const int y1 = min(cell_of(__fadd_rn(p.y, ui), o.y, g.cell), B.y0 + 2);
-    B.zlo = max(cell_of(__fsub_rn(p.z, ui), o.z, g.cell), B.zlo);
-    B.zhi = min(cell_of(__fadd_rn(p.z, ui), o.z, g.cell), B.zhi);
+    const float inv = g.inv_cell;
+    const int x0 = max(lo_cell(__fsub_rn(p.x, ui), o.x, inv), B.x0);
+    const int x1 = min(hi_cell(__fadd_rn(p.x, ui), o.x, inv), B.x0 + 2);
+    const int y0 = max(lo_cell(__fsub_rn(p.y, ui), o.y, inv), B.y0);
+    const int y1 = min(hi_cell(__fadd_rn(p.y, ui), o.y, inv), B.y0 + 2);
+    B.zlo = max(lo_cell(__fsub_rn(p.z, ui), o.z, inv), B.zlo);
+    B.zhi = min(hi_cell(__fadd_rn(p.z, ui), o.z, inv), B.zhi);
     // the ball contains p, so every range contains p's own cell: never empty
     B.x0 = x0, B.nx = x1 - x0 + 1;
     B.y0 = y0, B.ny = y1 - y0 + 1;
@@ -297,24 +312,21 @@ struct NNBest2
     float s2; // second-smallest squared distance, +inf when fewer than two points
 };
 
-// radius R of the ball around p whose points all lie in cells of box B: each
-// axis's bound is checked through cell_of itself, with p - R rounded down and
-// p + R rounded up (cell_of is monotonic, and it is how the grid binned its
-// points).  0 when no positive radius passes.
+// radius R of the ball around p whose points all lie in cells of box B: the
+// distance from p to the box's faces, less a slack that covers the rounding of
+// that distance and of the binning (cell_of is within 2 rounding units of
+// (v - o) / cell); 0 when nothing positive remains
 __device__ __forceinline__ float box_cover(const GridDev &g, float3 o, float3 p, const CellBox &B)
 {
     const float c = g.cell;
-    const float fx0 = o.x + (float)B.x0 * c, fx1 = o.x + (float)(B.x0 + B.nx) * c;
-    const float fy0 = o.y + (float)B.y0 * c, fy1 = o.y + (float)(B.y0 + B.ny) * c;
-    const float fz0 = o.z + (float)B.zlo * c, fz1 = o.z + (float)(B.zhi + 1) * c;
-    float r = fminf(fminf(fminf(p.x - fx0, fx1 - p.x), fminf(p.y - fy0, fy1 - p.y)), fminf(p.z - fz0, fz1 - p.z));
-    r = r * 0.99998f - 1e-6f * (1.0f + fmaxf(fmaxf(fabsf(p.x), fabsf(p.y)), fabsf(p.z)));
-    if (!(r > 0.0f))
-        return 0.0f;
-    const bool ok = cell_of(__fsub_rd(p.x, r), o.x, c) >= B.x0 && cell_of(__fadd_ru(p.x, r), o.x, c) < B.x0 + B.nx &&
-                    cell_of(__fsub_rd(p.y, r), o.y, c) >= B.y0 && cell_of(__fadd_ru(p.y, r), o.y, c) < B.y0 + B.ny &&
-                    cell_of(__fsub_rd(p.z, r), o.z, c) >= B.zlo && cell_of(__fadd_ru(p.z, r), o.z, c) <= B.zhi;
-    return ok ? r : 0.0f;
+    auto axis = [c](float pv, float ov, int lo, int n) {
+        const float d = pv - ov;
+        const float slack = 2e-6f * (fabsf(d) + fabsf(ov) + 3.0f * c);
+        return fminf(d - (float)lo * c, (float)(lo + n) * c - d) - slack;
+    };
+    const float r = fminf(fminf(axis(p.x, o.x, B.x0, B.nx), axis(p.y, o.y, B.y0, B.ny)),
+                          axis(p.z, o.z, B.zlo, B.zhi - B.zlo + 1));
+    return r > 0.0f ? r * 0.99999f : 0.0f;
 }
 
 // the nearest grid point inside box B at any distance (ties to the smaller original

@@ -264,6 +264,7 @@ struct KeyLayout
 {
     int bseg, bx, by, bz; // bits per field; key = seg|cx|cy|cz from MSB to LSB
     int total_bits;
+    int morton; // voxel keys only: seg | bit-interleaved (cx, cy, cz), bx = by = bz
 };
 
 // one open-addressing slot of the row hash: the key and the row's [start, end) in
@@ -280,7 +281,8 @@ struct GridDev
 {
     // per segment
     float3 *gmin;  // grid origin
-    float cell;    // cell edge
+    float cell;     // cell edge
+    float inv_cell; // 1 / cell (conservative bounds only; cells are assigned by division)
     KeyLayout *layout;
     // sorted points (global positions over all segments)
     float4 *spos;  // x, y, z, __int_as_float(cz)

@@ -101,7 +101,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         Batch bs, bt;
         if (S.voxel > 0.0f)
         {
-            if ((st = voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs)))
+            if ((st = voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true)))
                 return st;
             if ((st = voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt)))
                 return st;

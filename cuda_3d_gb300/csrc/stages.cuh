@@ -87,8 +87,10 @@ int cloud_batch(gca3d_context *ctx, gca3d_cloud *c, Batch &b);
 int batch_alloc(gca3d_context *ctx, Batch &b, int P, int64_t cap, int64_t max_seg_cap, bool nrm, bool grd);
 
 // stage 0 of a scale: voxel downsample (voxel > 0) or gather copy into a batch
+// morton: output in Z-order of the voxels instead of the reference's (x, y, z) order
+// (same voxels, same centroids)
 int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap, int64_t max_seg_cap,
-                float voxel, Batch &out);
+                float voxel, Batch &out, bool morton = false);
 int gather_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t max_seg_cap, Batch &out,
                  bool with_normals);
 

@@ -93,8 +93,13 @@ __global__ void k_src_bounds(const SegSrc *src, int *ord)
     block_bounds_commit(mn, mx, ord + 6 * seg);
 }
 
-// key layout shared by all segments; per-segment origin = unpadded aabb min
-__global__ void k_voxel_layout(const int *ord, int P, float voxel, float3 *origin, KeyLayout *lay, int *d_err)
+// key layout shared by all segments; per-segment origin = unpadded aabb min.  With
+// morton (and room in 64 bits) the three axis keys are bit-interleaved below the
+// segment index instead: the voxels then come out in Z-order, so runs of
+// consecutive output points are compact in space (the correspondence search of the
+// ICP stages a block's target cells once for such a run).
+__global__ void k_voxel_layout(const int *ord, int P, float voxel, bool morton, float3 *origin, KeyLayout *lay,
+                               int *d_err)
 {
     __shared__ uint32_t s_max[3];
     if (threadIdx.x < 3)
@@ -131,10 +136,30 @@ __global__ void k_voxel_layout(const int *ord, int P, float voxel, float3 *origi
         L.by = max(1, bitlen_u32(s_max[1]));
         L.bz = max(1, bitlen_u32(s_max[2]));
         L.total_bits = L.bseg + L.bx + L.by + L.bz;
+        L.morton = 0;
+        const int b = max(L.bx, max(L.by, L.bz));
+        if (morton && L.bseg + 3 * b <= 64)
+        {
+            L.bx = L.by = L.bz = b;
+            L.total_bits = L.bseg + 3 * b;
+            L.morton = 1;
+        }
         if (L.total_bits > 64)
             atomicOr(d_err, kErrKeyBits);
         *lay = L;
     }
+}
+
+// the bits of v (up to 21) at every third position (bit interleaving by masks)
+__device__ __forceinline__ uint64_t spread3(uint64_t v)
+{
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
 }
 
 __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3 *origin, const KeyLayout *lay,
@@ -151,7 +176,9 @@ __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3
         float4 p = pos[i];
         uint64_t kx = (uint32_t)cell_of(p.x, o.x, voxel), ky = (uint32_t)cell_of(p.y, o.y, voxel),
                  kz = (uint32_t)cell_of(p.z, o.z, voxel);
-        uint64_t key = ((uint64_t)seg << (L.bx + L.by + L.bz)) | (kx << (L.by + L.bz)) | (ky << L.bz) | kz;
+        const uint64_t key = ((uint64_t)seg << (L.bx + L.by + L.bz)) |
+                             (L.morton ? (spread3(kx) << 2) | (spread3(ky) << 1) | spread3(kz)
+                                       : (kx << (L.by + L.bz)) | (ky << L.bz) | kz);
         keys[base + i] = key;
         vals[base + i] = base + i;
     }
@@ -240,7 +267,7 @@ __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuf
 }
 
 int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap, int64_t max_seg_cap,
-                float voxel, Batch &out)
+                float voxel, Batch &out, bool morton)
 {
     if (!(voxel > 0.0f))
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "voxel size must be > 0");
@@ -278,7 +305,7 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     const int gx = std::min(grid_for(max_seg_cap, kBlock * 4), ctx->num_sms * 4);
     k_src_bounds<<<dim3(gx, P), kBlock, 0, s>>>(d_src, ord);
     GCA_CHECK_LAUNCH(ctx);
-    k_voxel_layout<<<1, 256, 0, s>>>(ord, P, voxel, origin, lay, ctx->d_err);
+    k_voxel_layout<<<1, 256, 0, s>>>(ord, P, voxel, morton, origin, lay, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     k_voxel_keys<<<dim3(gx, P), kBlock, 0, s>>>(d_src, in_off, origin, lay, voxel, sb.keys[0], sb.vals[0]);
     GCA_CHECK_LAUNCH(ctx);
