@@ -420,54 +420,75 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
             s_S[k] = Comp ? v : (double)vf;
         }
         __syncthreads();
-        if (threadIdx.x == 0)
+        const int warp = grp;
+        if (warp == 0)
         {
-            double S[kTerms];
-            for (int k = 0; k < kTerms; ++k)
-                S[k] = s_S[k];
-            const double ns = (double)Ps.nsrc;
-            Ps.rmse_ref = S[27] / ns;
-            Ps.fitness = S[28] / ns;
-            Ps.inlier_rmse = S[28] > 0.0 ? sqrt(S[29] / S[28]) : 0.0;
-            double x[6], Ti[16];
-            const int singular = solve6_device(S, x);
-            if (prm.trace && Ps.iters < prm.trace_cap)
+            // solve, step map and composition over the lanes of warp 0
+            double x[6];
+            const int singular = solve6_warp(s_S, x);
+            const double Ti = pose_from_x_warp(x, prm.update_map); // lanes 0..15: Ti[lane]
+            const int r = (lane >> 2) & 3, c = lane & 3;
+            const double Told = lane < 16 ? Ps.T[lane] : 0.0;
+            double v = 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                v += __shfl_sync(0xffffffffu, Ti, 4 * r + k) * __shfl_sync(0xffffffffu, Told, 4 * k + c);
+            const double t00 = __shfl_sync(0xffffffffu, Ti, 0), t11 = __shfl_sync(0xffffffffu, Ti, 5),
+                         t22 = __shfl_sync(0xffffffffu, Ti, 10), t03 = __shfl_sync(0xffffffffu, Ti, 3),
+                         t13 = __shfl_sync(0xffffffffu, Ti, 7), t23 = __shfl_sync(0xffffffffu, Ti, 11);
+            const int iters = Ps.iters;
+            if (prm.trace && iters < prm.trace_cap)
             {
-                IcpTrace &tr = prm.trace[(size_t)Ps.iters * P + pair];
-                for (int k = 0; k < 16; ++k)
-                    tr.T[k] = Ps.T[k];
-                for (int k = 0; k < kTerms; ++k)
-                    tr.S[k] = S[k];
-                for (int k = 0; k < 6; ++k)
-                    tr.x[k] = x[k];
-                tr.status = singular;
-            }
-            if (S[28] == 0.0)
-                Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
-            else if (singular && Ps.status == 0)
-                Ps.status = GCA3D_ERR_SINGULAR;
-            pose_from_x_device(x, prm.update_map, Ti);
-            double Tn[16];
-            for (int r = 0; r < 4; ++r)
-                for (int c = 0; c < 4; ++c)
+                IcpTrace &tr = prm.trace[(size_t)iters * P + pair];
+                if (lane < 16)
+                    tr.T[lane] = Told;
+                if (lane < kTerms)
+                    tr.S[lane] = s_S[lane];
+                if (lane == 0)
                 {
-                    double v = 0.0;
-                    for (int k = 0; k < 4; ++k)
-                        v += Ti[4 * r + k] * Ps.T[4 * k + c];
-                    Tn[4 * r + c] = v;
+#pragma unroll
+                    for (int q = 0; q < 6; ++q)
+                        tr.x[q] = x[q];
+                    tr.status = singular;
                 }
-            for (int k = 0; k < 16; ++k)
-                Ps.T[k] = Tn[k];
-            Ps.iters += 1;
-            Ps.scale_iters[Ps.scale] += 1;
-            Ps.nn_warm = 1;
-            const double cth = 0.5 * (Ti[0] + Ti[5] + Ti[10] - 1.0);
-            const double tsq = Ti[3] * Ti[3] + Ti[7] * Ti[7] + Ti[11] * Ti[11];
-            if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
-            {
-                Ps.converged = 1;
-                Ps.active = 0;
             }
+            __syncwarp();
+            if (lane < 16)
+                Ps.T[lane] = v;
+            if (lane == 0)
+            {
+                if (s_S[28] == 0.0)
+                    Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
+                else if (singular && Ps.status == 0)
+                    Ps.status = GCA3D_ERR_SINGULAR;
+                Ps.iters = iters + 1;
+                Ps.scale_iters[Ps.scale] += 1;
+                Ps.nn_warm = 1;
+                const double cth = 0.5 * (t00 + t11 + t22 - 1.0);
+                const double tsq = t03 * t03 + t13 * t13 + t23 * t23;
+                if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
+                {
+                    Ps.converged = 1;
+                    Ps.active = 0;
+                }
+            }
+        }
+        else if (warp == 1)
+        {
+            // the statistics, on their own warp (one division per lane)
+            const double ns = (double)Ps.nsrc;
+            const int m = lane % 3;
+            const double num = m == 0 ? s_S[27] : (m == 1 ? s_S[28] : s_S[29]);
+            const double den = m == 2 ? s_S[28] : ns;
+            double q = num / den;
+            if (m == 2)
+                q = s_S[28] > 0.0 ? sqrt(q) : 0.0;
+            if (lane == 0)
+                Ps.rmse_ref = q;
+            else if (lane == 1)
+                Ps.fitness = q;
+            else if (lane == 2)
+                Ps.inlier_rmse = q;
         }
     }
     // the last block: work maps over the pairs still active (the next iteration's

@@ -11,9 +11,9 @@
 // E[xx^T] - E[x]E[x]^T does).  The 3x3 eigen-problem is solved in closed form in
 // FP32; points whose two smallest eigenvalues are close (about 0.2 % of surface
 // points) are queued and redone by a second kernel with the covariance rebuilt in
-// FP64 and Jacobi rotations -- densely, one point per thread, because FP64 issues
-// at a small fraction of the FP32 rate here and a divergent fallback inside the
-// FP32 kernel would stall whole warps.  A third kernel computes the gradients.  The gradient follows the reference's
+// FP64 and a closed-form FP64 eigen-solve -- densely, one point per thread, because
+// FP64 issues at a small fraction of the FP32 rate here and a divergent fallback
+// inside the FP32 kernel would stall whole warps.  A third kernel computes the gradients.  The gradient follows the reference's
 // system: tangent-plane least squares, (knn - 1)^2 n n^T orthogonality term,
 // 1e-6 ridge, LDL^T solve (in the tangent/normal basis, see solve_gradient_system).
 #include "grid_query.cuh"
@@ -26,52 +26,104 @@ namespace gca3d
 
 constexpr int kMaxNN = 64;
 
-// FP64 Jacobi eigenvector of the smallest eigenvalue (same sweeps as the oracle)
-__device__ void jacobi_smallest(double a[3][3], double out[3])
+// FP64 eigenvector of the smallest eigenvalue of a symmetric 3x3 whose two smallest
+// eigenvalues may be close (the points the FP32 pass queues).  The largest
+// eigenvalue is then well separated: it comes from the trigonometric formula and
+// its eigenvector v1 from the largest cross product of the rows of A - l1 I.  The
+// other two eigenvectors span the plane orthogonal to v1; in an orthonormal basis
+// (u, w) of that plane A is a 2x2 symmetric matrix, which one rotation (the
+// Jacobi rotation of the oracle's sweeps) diagonalises exactly.  The result is
+// accurate to eps / gap like the sweeps, at about a quarter of their FP64
+// instructions (FP64 issues at a small fraction of the FP32 rate here, and this is
+// one thread's dependent chain).  An isotropic matrix gives (1, 0, 0), as the
+// sweeps do (no rotation, first of equal diagonal entries).
+__device__ void smallest_eigvec_f64(const double A[3][3], double out[3])
 {
-    double V[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    for (int sweep = 0; sweep < 64; ++sweep)
+    double m = 0.0;
+    for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j)
+            m = fmax(m, fabs(A[i][j]));
+    out[0] = 1.0, out[1] = 0.0, out[2] = 0.0;
+    if (!(m > 0.0))
+        return;
+    const double inv = 1.0 / m;
+    const double a00 = A[0][0] * inv, a01 = A[0][1] * inv, a02 = A[0][2] * inv;
+    const double a11 = A[1][1] * inv, a12 = A[1][2] * inv, a22 = A[2][2] * inv;
+    const double q = (a00 + a11 + a22) * (1.0 / 3.0);
+    const double b00 = a00 - q, b11 = a11 - q, b22 = a22 - q;
+    const double p2 = (b00 * b00 + b11 * b11 + b22 * b22 + 2.0 * (a01 * a01 + a02 * a02 + a12 * a12)) * (1.0 / 6.0);
+    if (!(p2 > 0.0))
+        return;
+    const double p = sqrt(p2);
+    const double det = b00 * (b11 * b22 - a12 * a12) - a01 * (a01 * b22 - a12 * a02) + a02 * (a01 * a12 - b11 * a02);
+    const double r = fmin(fmax(det / (2.0 * p2 * p), -1.0), 1.0);
+    const double l1 = q + 2.0 * p * cos(acos(r) * (1.0 / 3.0));
+    // v1: the null vector of A - l1 I
+    const double r0[3] = {a00 - l1, a01, a02}, r1[3] = {a01, a11 - l1, a12}, r2[3] = {a02, a12, a22 - l1};
+    auto cross = [](const double *x, const double *y, double *z) {
+        z[0] = x[1] * y[2] - x[2] * y[1];
+        z[1] = x[2] * y[0] - x[0] * y[2];
+        z[2] = x[0] * y[1] - x[1] * y[0];
+    };
+    double c0[3], c1[3], c2[3];
+    cross(r0, r1, c0);
+    cross(r0, r2, c1);
+    cross(r1, r2, c2);
+    const double d0 = c0[0] * c0[0] + c0[1] * c0[1] + c0[2] * c0[2];
+    const double d1 = c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2];
+    const double d2 = c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2];
+    const double *c = c0;
+    double dm = d0;
+    if (d1 > dm)
+        c = c1, dm = d1;
+    if (d2 > dm)
+        c = c2, dm = d2;
+    if (!(dm > 0.0))
+        return;
+    const double il = 1.0 / sqrt(dm);
+    const double v1[3] = {c[0] * il, c[1] * il, c[2] * il};
+    // orthonormal basis (u, w) of the plane orthogonal to v1
+    double u[3];
+    if (fabs(v1[0]) > fabs(v1[1]))
     {
-        double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
-        double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
-        if (off <= 1e-36 * diag || off == 0.0)
-            break;
-        for (int p = 0; p < 2; ++p)
-            for (int q = p + 1; q < 3; ++q)
-            {
-                if (a[p][q] == 0.0)
-                    continue;
-                double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; ++k)
-                {
-                    double akp = a[k][p], akq = a[k][q];
-                    a[k][p] = c * akp - s * akq;
-                    a[k][q] = s * akp + c * akq;
-                }
-                for (int k = 0; k < 3; ++k)
-                {
-                    double apk = a[p][k], aqk = a[q][k];
-                    a[p][k] = c * apk - s * aqk;
-                    a[q][k] = s * apk + c * aqk;
-                }
-                for (int k = 0; k < 3; ++k)
-                {
-                    double vkp = V[k][p], vkq = V[k][q];
-                    V[k][p] = c * vkp - s * vkq;
-                    V[k][q] = s * vkp + c * vkq;
-                }
-            }
+        const double iu = 1.0 / sqrt(v1[0] * v1[0] + v1[2] * v1[2]);
+        u[0] = -v1[2] * iu, u[1] = 0.0, u[2] = v1[0] * iu;
     }
-    int s = 0;
-    for (int k = 1; k < 3; ++k)
-        if (a[k][k] < a[s][s])
-            s = k;
-    double l = sqrt(V[0][s] * V[0][s] + V[1][s] * V[1][s] + V[2][s] * V[2][s]);
-    out[0] = V[0][s] / l;
-    out[1] = V[1][s] / l;
-    out[2] = V[2][s] / l;
+    else
+    {
+        const double iu = 1.0 / sqrt(v1[1] * v1[1] + v1[2] * v1[2]);
+        u[0] = 0.0, u[1] = v1[2] * iu, u[2] = -v1[1] * iu;
+    }
+    double w[3];
+    cross(v1, u, w);
+    const double Au[3] = {a00 * u[0] + a01 * u[1] + a02 * u[2], a01 * u[0] + a11 * u[1] + a12 * u[2],
+                          a02 * u[0] + a12 * u[1] + a22 * u[2]};
+    const double Aw[3] = {a00 * w[0] + a01 * w[1] + a02 * w[2], a01 * w[0] + a11 * w[1] + a12 * w[2],
+                          a02 * w[0] + a12 * w[1] + a22 * w[2]};
+    const double m00 = u[0] * Au[0] + u[1] * Au[1] + u[2] * Au[2];
+    const double m01 = u[0] * Aw[0] + u[1] * Aw[1] + u[2] * Aw[2];
+    const double m11 = w[0] * Aw[0] + w[1] * Aw[1] + w[2] * Aw[2];
+    double e[3];
+    if (m01 == 0.0)
+    {
+        const double *s = m00 <= m11 ? u : w;
+        e[0] = s[0], e[1] = s[1], e[2] = s[2];
+    }
+    else
+    {
+        // rotation by (c, s): eigenvalue m00 - t m01 on c u - s w, m11 + t m01 on s u + c w
+        const double theta = (m11 - m00) / (2.0 * m01);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double cr = 1.0 / sqrt(t * t + 1.0), sr = t * cr;
+        if (m00 - t * m01 <= m11 + t * m01)
+            for (int k = 0; k < 3; ++k)
+                e[k] = cr * u[k] - sr * w[k];
+        else
+            for (int k = 0; k < 3; ++k)
+                e[k] = sr * u[k] + cr * w[k];
+    }
+    const double ie = 1.0 / sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+    out[0] = e[0] * ie, out[1] = e[1] * ie, out[2] = e[2] * ie;
 }
 
 // closed-form symmetric 3x3 eigen-system (trigonometric eigenvalues, eigenvector
@@ -291,7 +343,8 @@ __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n
 }
 
 // pass 2: the queued near-degenerate points, one per thread (no divergence with
-// the FP32 majority): covariance rebuilt in FP64 from the same neighbours, Jacobi
+// the FP32 majority): covariance rebuilt in FP64 from the same neighbours,
+// closed-form FP64 eigenvector
 __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_nn, NormalOut O)
 {
     const int n = *O.degen_count;
@@ -340,7 +393,7 @@ __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_
         C[1][2] = C[2][1] = S2[4] / kk - mu[1] * mu[2];
         C[2][2] = S2[5] / kk - mu[2] * mu[2];
         double v[3];
-        jacobi_smallest(C, v);
+        smallest_eigvec_f64(C, v);
         float3 nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
         if (nrm.z > 0.0f)
             nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);

@@ -164,6 +164,198 @@ __device__ inline int solve6_device(const double *S /* 21 upper + 6 rhs */, doub
     return status;
 }
 
+// ---------------------------------------------------------------------------
+// Warp-parallel restatements of solve6_device and pose_from_x_device for the
+// per-iteration finalize.  FP64 issues at a small fraction of the FP32 rate on
+// this part, so a single thread's dependent FP64 chain costs tens of
+// microseconds; spread over the lanes of a warp, the chain is the depth of the
+// computation instead of its length.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int tri_lane(int i, int j) { return i * (i + 1) / 2 + j; } // i >= j
+
+// solve6_device over one warp (same symmetric pivots, factorisation and
+// substitutions; the backward substitution sums in the opposite order).  Lane
+// tri_lane(i, j) < 21 holds A[i][j] of the lower triangle, lanes 21..26 the
+// right-hand side.  All 32 lanes call it; every lane returns the status and x.
+__device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double x[6])
+{
+    constexpr double kTiny = 2.2250738585072014e-308;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int li = 0;
+    while (li < 5 && tri_lane(li + 1, 0) <= lane)
+        ++li;
+    const int lj = lane - tri_lane(li, 0);
+    const bool mat = lane < 21, diag = mat && li == lj;
+    double a = 0.0;
+    if (mat)
+        a = S[lj * 6 - lj * (lj - 1) / 2 + (li - lj)]; // upper-packed (lj, li)
+    else if (lane < 27)
+        a = -S[lane];
+    const bool bad = lane < 27 && !isfinite(a);
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+        x[q] = 0.0;
+    if (__any_sync(full, bad))
+        return 1;
+    unsigned perm = 0x543210u; // 4 bits per entry
+    int status = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+    {
+        // symmetric pivot: the largest remaining diagonal entry (first one on ties);
+        // magnitudes compared as the bit patterns of |A[i][i]|
+        const long long mag = diag ? (__double_as_longlong(a) & 0x7fffffffffffffffll) : -1ll;
+        int piv = k;
+        long long best = __shfl_sync(full, mag, tri_lane(k, k));
+#pragma unroll
+        for (int i = k + 1; i < 6; ++i)
+        {
+            const long long v = __shfl_sync(full, mag, tri_lane(i, i));
+            if (v > best)
+            {
+                best = v;
+                piv = i;
+            }
+        }
+        if (piv != k)
+        {
+            const int si = li == k ? piv : (li == piv ? k : li), sj = lj == k ? piv : (lj == piv ? k : lj);
+            const int src = mat ? tri_lane(max(si, sj), min(si, sj)) : lane;
+            a = __shfl_sync(full, a, src);
+            const unsigned pk = (perm >> (4 * k)) & 15u, pp = (perm >> (4 * piv)) & 15u;
+            perm = (perm & ~((15u << (4 * k)) | (15u << (4 * piv)))) | (pp << (4 * k)) | (pk << (4 * piv));
+        }
+        const double Dk = __shfl_sync(full, a, tri_lane(k, k));
+        const bool lcol = mat && lj == k && li > k;
+        if (fabs(Dk) <= kTiny)
+        {
+            status = 1;
+            if (lcol)
+                a = 0.0;
+        }
+        else
+        {
+            const double inv = 1.0 / Dk; // one reciprocal per pivot, as solve6_device
+            if (lcol)
+                a *= inv;
+            const bool upd = mat && lj > k;
+            const double lik = __shfl_sync(full, a, upd ? tri_lane(li, k) : lane);
+            const double ljk = __shfl_sync(full, a, upd ? tri_lane(lj, k) : lane);
+            if (upd)
+                a -= lik * ljk * Dk;
+        }
+    }
+    // L y = P b (the diagonal lanes accumulate), then y / D
+    const int pi = (int)((perm >> (4 * li)) & 15u);
+    double acc = __shfl_sync(full, a, diag ? 21 + pi : lane);
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+    {
+        const double yj = __shfl_sync(full, acc, tri_lane(j, j));
+        const double lij = __shfl_sync(full, a, diag && li > j ? tri_lane(li, j) : lane);
+        if (diag && li > j)
+            acc -= lij * yj;
+    }
+    if (diag)
+        acc = fabs(a) > kTiny ? acc / a : 0.0;
+    // L^T z = y, by columns from the last
+#pragma unroll
+    for (int j = 5; j > 0; --j)
+    {
+        const double zj = __shfl_sync(full, acc, tri_lane(j, j));
+        const double lji = __shfl_sync(full, a, diag && li < j ? tri_lane(j, li) : lane);
+        if (diag && li < j)
+            acc -= lji * zj;
+    }
+    // x[perm[i]] = z[i]
+    unsigned invp = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+        invp |= (unsigned)i << (4 * ((perm >> (4 * i)) & 15u));
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+    {
+        const int iq = (int)((invp >> (4 * q)) & 15u);
+        x[q] = __shfl_sync(full, acc, tri_lane(iq, iq));
+    }
+    return status;
+}
+
+// pose_from_x_device over one warp: every lane returns Ti[lane] for lane < 16
+// (row-major 4x4), the same formulas with the three sines and cosines of the
+// Euler map (or the coefficient divisions of the exponential) on separate lanes
+// and one matrix entry per lane.
+__device__ inline double pose_from_x_warp(const double x[6], int map)
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int r = (lane >> 2) & 3, c = lane & 3; // the Ti entry of this lane
+    const int rr = min(r, 2), cc = min(c, 2);  // its 3x3 entry (clamped for the 4th row / column)
+    double Rrc, tr;
+    if (map == GCA3D_UPDATE_EULER_ZYX)
+    {
+        const int m = lane % 3;
+        const double xm = m == 0 ? x[0] : (m == 1 ? x[1] : x[2]);
+        double sn, cs;
+        sincos(xm, &sn, &cs);
+        const double sa = __shfl_sync(full, sn, 0), ca = __shfl_sync(full, cs, 0);
+        const double sb = __shfl_sync(full, sn, 1), cb = __shfl_sync(full, cs, 1);
+        const double sc = __shfl_sync(full, sn, 2), ccz = __shfl_sync(full, cs, 2);
+        // R = Rz(x2) Ry(x1) Rx(x0), entry (rr, cc) as u * v * w + g0 * g1 with
+        // operands picked per lane (one uniform FP64 expression, no divergence)
+        const int e = 3 * rr + cc;
+        const double u = rr == 0 ? ccz : (rr == 1 ? sc : (cc == 0 ? -sb : cb));
+        const double v = e == 0 || e == 3 ? cb : (e == 6 ? 1.0 : (rr == 2 ? (cc == 1 ? sa : ca) : sb));
+        const double w = cc == 0 || rr == 2 ? 1.0 : (cc == 1 ? sa : ca);
+        const double g0 = cc == 0 || rr == 2 ? 0.0 : (e == 1 ? -sc : (e == 2 ? sc : (e == 4 ? ccz : -ccz)));
+        const double g1 = cc == 0 || rr == 2 ? 0.0 : (cc == 1 ? ca : sa);
+        Rrc = u * v * w + g0 * g1;
+        tr = rr == 0 ? x[3] : (rr == 1 ? x[4] : x[5]);
+    }
+    else
+    {
+        const double w0 = x[0], w1 = x[1], w2 = x[2];
+        const double th2 = w0 * w0 + w1 * w1 + w2 * w2, th = sqrt(th2);
+        double A, B, C;
+        if (th < 1e-4)
+        {
+            A = 1.0 - th2 / 6.0 + th2 * th2 / 120.0;
+            B = 0.5 - th2 / 24.0 + th2 * th2 / 720.0;
+            C = 1.0 / 6.0 - th2 / 120.0 + th2 * th2 / 5040.0;
+        }
+        else
+        {
+            double sn, cs;
+            sincos(th, &sn, &cs);
+            // the three coefficient divisions on three lanes
+            const int m = lane % 3;
+            const double num = m == 0 ? sn : (m == 1 ? 1.0 - cs : th - sn);
+            const double den = m == 0 ? th : (m == 1 ? th2 : th2 * th);
+            const double q = num / den;
+            A = __shfl_sync(full, q, 0);
+            B = __shfl_sync(full, q, 1);
+            C = __shfl_sync(full, q, 2);
+        }
+        const double K[3][3] = {{0, -w2, w1}, {w2, 0, -w0}, {-w1, w0, 0}};
+        auto Kat = [&](int i, int j) { return i == 0 ? (j == 0 ? K[0][0] : j == 1 ? K[0][1] : K[0][2])
+                                             : i == 1 ? (j == 0 ? K[1][0] : j == 1 ? K[1][1] : K[1][2])
+                                                      : (j == 0 ? K[2][0] : j == 1 ? K[2][1] : K[2][2]); };
+        const double Kij = Kat(rr, cc);
+        const double k2 = Kat(rr, 0) * Kat(0, cc) + Kat(rr, 1) * Kat(1, cc) + Kat(rr, 2) * Kat(2, cc);
+        const double I = rr == cc ? 1.0 : 0.0;
+        Rrc = I + A * Kij + B * k2;
+        const double Vrc = I + B * Kij + C * k2; // this lane's V entry (rr, cc)
+        // t[rr] = V[rr][0] x3 + V[rr][1] x4 + V[rr][2] x5, V from the lanes 4 rr + 0..2
+        const double v0 = __shfl_sync(full, Vrc, 4 * rr), v1 = __shfl_sync(full, Vrc, 4 * rr + 1),
+                     v2 = __shfl_sync(full, Vrc, 4 * rr + 2);
+        tr = v0 * x[3] + v1 * x[4] + v2 * x[5];
+    }
+    if (r == 3)
+        return c == 3 ? 1.0 : 0.0;
+    return c == 3 ? tr : Rrc;
+}
+
 __device__ inline void pose_from_x_device(const double x[6], int map, double T[16])
 {
     double R[3][3], t[3];

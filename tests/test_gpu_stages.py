@@ -216,6 +216,38 @@ def test_normals_vs_f64(ctx, orc, room_v01, max_nn):
     np.testing.assert_allclose(np.linalg.norm(n[ok], axis=1), 1.0, atol=1e-5)
 
 
+def test_degenerate_normals_vs_f64(ctx, orc):
+    """Points on thin noisy lines: the two smallest eigenvalues of every
+    neighbourhood are close, so the FP32 pass queues them and every normal comes
+    from the FP64 pass.  Where the gap is resolvable and well inside the FP32
+    pass's 1e-3 threshold (relative gap of the two smallest eigenvalues between
+    1e-7 and 3e-4) the normal is determined to about 1e-16 / gap and must match the
+    oracle's FP64 sweeps."""
+    cKDTree = pytest.importorskip("scipy.spatial").cKDTree
+
+    rng = np.random.default_rng(3)
+    lines = []
+    for _ in range(20):
+        o = rng.uniform(-1.0, 1.0, 3)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        t = rng.uniform(0.0, 0.5, 300)
+        lines.append(o + t[:, None] * d + rng.normal(size=(300, 3)) * 2e-4)
+    xyz = np.concatenate(lines).astype(np.float32)
+    n = normals_gpu(ctx, xyz, 0.02)
+    ref = orc.normals_f64(xyz, 0.02, 0)
+    x64 = xyz.astype(np.float64)
+    gap = np.full(len(xyz), np.nan)
+    for i, nb in enumerate(cKDTree(x64).query_ball_point(x64, 0.0199)):
+        if len(nb) >= 3:
+            ev = np.linalg.eigvalsh(np.cov(x64[nb].T, bias=True))
+            gap[i] = (ev[1] - ev[0]) / (ev[2] - ev[0])
+    sel = (gap > 1e-7) & (gap < 3e-4)
+    assert sel.sum() > 500
+    err = angle_err(n[sel].astype(np.float64), ref[sel])
+    assert err.max() < 1e-6, np.percentile(err, [50, 99, 100])
+
+
 def test_gradient_vs_f64(ctx, orc, room_v01):
     xyz, rgb = room_v01
     c = ctx.cloud_from(xyz, rgb)
