@@ -9,11 +9,12 @@
 // registers; no lists exist.  Moments are taken about the query point, so the
 // FP32 covariance does not cancel at metre-scale coordinates (the reference's
 // E[xx^T] - E[x]E[x]^T does).  The 3x3 eigen-problem is solved in closed form in
-// FP32; points whose two smallest eigenvalues are close (about 0.2 % of surface
-// points) are queued and redone by a second kernel with the covariance rebuilt in
-// FP64 and a closed-form FP64 eigen-solve -- densely, one point per thread, because
-// FP64 issues at a small fraction of the FP32 rate here and a divergent fallback
-// inside the FP32 kernel would stall whole warps.  A third kernel computes the gradients.  The gradient follows the reference's
+// FP32; points whose two smallest eigenvalues are close (a few dozen per frame)
+// are queued and redone by a second kernel with the covariance rebuilt in FP64
+// and a closed-form FP64 eigen-solve, one warp per point (FP64 issues at a small
+// fraction of the FP32 rate here, so the work is spread over lanes, and a
+// divergent fallback inside the FP32 kernel would stall whole warps).  A third
+// kernel computes the gradients.  The gradient follows the reference's
 // system: tangent-plane least squares, (knn - 1)^2 n n^T orthogonality term,
 // 1e-6 ridge, LDL^T solve (in the tangent/normal basis, see solve_gradient_system).
 #include "grid_query.cuh"
@@ -342,17 +343,27 @@ __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n
     }
 }
 
-// pass 2: the queued near-degenerate points, one per thread (no divergence with
-// the FP32 majority): covariance rebuilt in FP64 from the same neighbours,
-// closed-form FP64 eigenvector
+// pass 2: the queued near-degenerate points (a few dozen per frame), one warp per
+// point: lanes 0..8 walk one row each of the 27-cell neighbourhood and write the
+// points inside the radius to shared memory at deterministic positions (row
+// counts, then their prefix); with max_nn the max_nn nearest (distance, then
+// index) are kept by rank; the FP64 moments about the point are summed per lane
+// and across the warp in a fixed order, and lane 0 solves the eigen-problem in
+// closed form.  A neighbourhood larger than the shared list (kN64Cand points)
+// falls back to one lane walking the rows itself.
+constexpr int kN64Cand = 256;
+
 __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_nn, NormalOut O)
 {
+    __shared__ float s_d2[4][kN64Cand];
+    __shared__ int s_t[4][kN64Cand];
     const int n = *O.degen_count;
     const KeyLayout L = *g.layout;
     const int segshift = L.bx + L.by + L.bz;
     const float rn2 = __fmul_rn(rn, rn);
-    NbrEntry list[kMaxNN];
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    for (int j = blockIdx.x * 4 + warp; j < n; j += gridDim.x * 4)
     {
         const int s = O.degen_list[j];
         const float4 p4 = g.spos[s];
@@ -360,7 +371,52 @@ __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_
         const int seg = L.bseg ? (int)(g.skey[s] >> segshift) : 0;
         GridRows R;
         grid_rows(g, L, seg, g.gmin[seg], p, R);
-        double S1[3] = {0, 0, 0}, S2[6] = {0, 0, 0, 0, 0, 0};
+        // the z window of this lane's row
+        int t0 = 0, e = 0;
+        if (lane < 9)
+        {
+            t0 = R.r[0].x, e = R.r[0].y;
+#pragma unroll
+            for (int k = 1; k < 9; ++k)
+                if (lane == k)
+                    t0 = R.r[k].x, e = R.r[k].y;
+            int a = t0, b = e;
+            while (a < b)
+            {
+                const int m = (a + b) >> 1;
+                if (__ldg(&g.scz[m]) < R.lo)
+                    a = m + 1;
+                else
+                    b = m;
+            }
+            t0 = a;
+        }
+        auto inside = [&](int t, float &d2) {
+            const float4 q = __ldg(&g.spos[t]);
+            const int qz = __float_as_int(q.w);
+            d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+            return qz <= R.hi && d2 < rn2;
+        };
+        int cnt = 0;
+        for (int t = t0; t < e; ++t)
+        {
+            float d2;
+            if (__float_as_int(__ldg(&g.spos[t]).w) > R.hi)
+                break;
+            if (inside(t, d2))
+                ++cnt;
+        }
+        int off = cnt;
+#pragma unroll
+        for (int d = 1; d < 16; d <<= 1)
+        {
+            const int y = __shfl_up_sync(full, off, d);
+            if (lane >= d)
+                off += y;
+        }
+        const int total = __shfl_sync(full, off, 8);
+        off -= cnt;
+        double S1[3] = {0.0, 0.0, 0.0}, S2[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
         int k = 0;
         auto acc = [&](float4 q) {
             const double dx = (double)q.x - (double)p.x, dy = (double)q.y - (double)p.y, dz = (double)q.z - (double)p.z;
@@ -369,35 +425,92 @@ __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_
             S2[3] += dy * dy, S2[4] += dy * dz, S2[5] += dz * dz;
             ++k;
         };
-        grid_scan(g, R, [&](int t, float4 q) {
-            if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
-                acc(q);
-        });
-        if (max_nn > 0 && k > max_nn)
+        if (total <= kN64Cand)
         {
-            S1[0] = S1[1] = S1[2] = 0.0;
-            for (int i = 0; i < 6; ++i)
-                S2[i] = 0.0;
-            k = 0;
-            const int cnt = select_knn(g, R, p, rn2, max_nn, list);
-            for (int i = 0; i < cnt; ++i)
-                acc(g.spos[list[i].t]);
+            int w = off;
+            for (int t = t0; t < e; ++t)
+            {
+                float d2;
+                if (__float_as_int(__ldg(&g.spos[t]).w) > R.hi)
+                    break;
+                if (inside(t, d2))
+                {
+                    s_d2[warp][w] = d2;
+                    s_t[warp][w] = t;
+                    ++w;
+                }
+            }
+            __syncwarp();
+            const bool select = max_nn > 0 && total > max_nn;
+            for (int c = lane; c < total; c += 32)
+            {
+                const float dc = s_d2[warp][c];
+                const int tc = s_t[warp][c];
+                bool keep = true;
+                if (select)
+                {
+                    int rank = 0;
+                    for (int o = 0; o < total; ++o)
+                    {
+                        const float d2o = s_d2[warp][o];
+                        rank += d2o < dc || (d2o == dc && __ldg(&g.sidx[s_t[warp][o]]) < __ldg(&g.sidx[tc]));
+                    }
+                    keep = rank < max_nn;
+                }
+                if (keep)
+                    acc(__ldg(&g.spos[tc]));
+            }
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1)
+            {
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+                    S1[i] += __shfl_xor_sync(full, S1[i], d);
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+                    S2[i] += __shfl_xor_sync(full, S2[i], d);
+                k += __shfl_xor_sync(full, k, d);
+            }
+            __syncwarp(); // the list is rewritten by the next point
         }
-        const double kk = (double)k;
-        const double mu[3] = {S1[0] / kk, S1[1] / kk, S1[2] / kk};
-        double C[3][3];
-        C[0][0] = S2[0] / kk - mu[0] * mu[0];
-        C[0][1] = C[1][0] = S2[1] / kk - mu[0] * mu[1];
-        C[0][2] = C[2][0] = S2[2] / kk - mu[0] * mu[2];
-        C[1][1] = S2[3] / kk - mu[1] * mu[1];
-        C[1][2] = C[2][1] = S2[4] / kk - mu[1] * mu[2];
-        C[2][2] = S2[5] / kk - mu[2] * mu[2];
-        double v[3];
-        smallest_eigvec_f64(C, v);
-        float3 nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
-        if (nrm.z > 0.0f)
-            nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
-        store_normal(O, s, g.sidx[s], nrm, g.sint[s]);
+        else if (lane == 0)
+        {
+            // a neighbourhood larger than the shared list: one lane, as the FP32 pass
+            grid_scan(g, R, [&](int t, float4 q) {
+                if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                    acc(q);
+            });
+            if (max_nn > 0 && k > max_nn)
+            {
+                NbrEntry list[kMaxNN];
+                S1[0] = S1[1] = S1[2] = 0.0;
+                for (int i = 0; i < 6; ++i)
+                    S2[i] = 0.0;
+                k = 0;
+                const int cnt2 = select_knn(g, R, p, rn2, max_nn, list);
+                for (int i = 0; i < cnt2; ++i)
+                    acc(g.spos[list[i].t]);
+            }
+        }
+        if (lane == 0)
+        {
+            const double kk = (double)k;
+            const double mu[3] = {S1[0] / kk, S1[1] / kk, S1[2] / kk};
+            double C[3][3];
+            C[0][0] = S2[0] / kk - mu[0] * mu[0];
+            C[0][1] = C[1][0] = S2[1] / kk - mu[0] * mu[1];
+            C[0][2] = C[2][0] = S2[2] / kk - mu[0] * mu[2];
+            C[1][1] = S2[3] / kk - mu[1] * mu[1];
+            C[1][2] = C[2][1] = S2[4] / kk - mu[1] * mu[2];
+            C[2][2] = S2[5] / kk - mu[2] * mu[2];
+            double v[3];
+            smallest_eigvec_f64(C, v);
+            float3 nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
+            if (nrm.z > 0.0f)
+                nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+            store_normal(O, s, g.sidx[s], nrm, g.sint[s]);
+        }
+        __syncwarp();
     }
 }
 
@@ -510,7 +623,7 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
         GCA_CUDA(ctx, cudaMemsetAsync(O.degen_count, 0, sizeof(int), ctx->stream));
         k_normals32<<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
-        k_normals64<<<ctx->num_sms, 128, 0, ctx->stream>>>(g.dev, normal_radius, max_nn, O);
+        k_normals64<<<ctx->num_sms * 2, 128, 0, ctx->stream>>>(g.dev, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
     }
     if (do_grad)
