@@ -272,7 +272,63 @@ struct NormalOut
     float4 *nrm_out;  // original order {n, 0}, or null
     int *degen_count; // near-degenerate points, appended for the FP64 pass
     int *degen_list;
+    // fused colour gradients (when grad_r2 > 0): outputs as k_gradient's, and the
+    // gradient moments of the queued points (three float4 per queue slot)
+    float grad_r2;
+    float4 *attr1, *grd_out;
+    float4 *degen_mom;
 };
+
+// The colour gradient from moments about the point p: G = sum d d^T (xx, xy, xz, yy,
+// yz, zz) and m = sum d (I_q - I_p) over the points within the gradient radius
+// (knn of them, p included), d = q - p.  The reference's system (sum v v^T +
+// (knn - 1)^2 n n^T + 1e-6 I) x = sum v dI with v = d - (d . n) n has sum v v^T =
+// P G P and sum v dI = P m (P = I - n n^T), so the neighbours need not be walked
+// again once n is known.  In the orthonormal basis (t1, t2, n) of
+// solve_gradient_system the projected terms have no normal row or column: the
+// tangent block is t^T G t, the normal entry (knn - 1)^2 |n|^2 + 1e-6, and the
+// right-hand side (t1 . m, t2 . m, 0).
+__device__ __forceinline__ float3 gradient_from_moments(float g0, float g1, float g2, float g3, float g4, float g5,
+                                                        float3 m, int knn, float3 n)
+{
+    const float G[6] = {g0, g1, g2, g3, g4, g5};
+    if (knn < 5)
+        return make_float3(0.0f, 0.0f, 0.0f);
+    const float w = (float)((knn - 1) * (knn - 1));
+    const float nn = n.x * n.x + n.y * n.y + n.z * n.z;
+    if (!(nn > 0.0f))
+        return ldlt3(G[0] + 1.0e-6f, G[1], G[2], G[3] + 1.0e-6f, G[4], G[5] + 1.0e-6f, m.x, m.y, m.z);
+    float3 t1;
+    if (fabsf(n.x) > fabsf(n.y))
+    {
+        const float il = rsqrtf(n.x * n.x + n.z * n.z);
+        t1 = make_float3(-n.z * il, 0.0f, n.x * il);
+    }
+    else
+    {
+        const float il = rsqrtf(n.y * n.y + n.z * n.z);
+        t1 = make_float3(0.0f, n.z * il, -n.y * il);
+    }
+    const float3 t2 = make_float3(n.y * t1.z - n.z * t1.y, n.z * t1.x - n.x * t1.z, n.x * t1.y - n.y * t1.x);
+    auto Gx = [&](float3 v) {
+        return make_float3(G[0] * v.x + G[1] * v.y + G[2] * v.z, G[1] * v.x + G[3] * v.y + G[4] * v.z,
+                           G[2] * v.x + G[4] * v.y + G[5] * v.z);
+    };
+    auto dot3 = [](float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; };
+    const float3 Gt1 = Gx(t1), Gt2 = Gx(t2);
+    const float3 y = ldlt3(dot3(t1, Gt1) + 1.0e-6f, dot3(t1, Gt2), 0.0f, dot3(t2, Gt2) + 1.0e-6f, 0.0f,
+                           w * nn + 1.0e-6f, dot3(t1, m), dot3(t2, m), 0.0f);
+    return make_float3(y.x * t1.x + y.y * t2.x + y.z * n.x, y.x * t1.y + y.y * t2.y + y.z * n.y,
+                       y.x * t1.z + y.y * t2.z + y.z * n.z);
+}
+
+__device__ __forceinline__ void store_gradient(const NormalOut &O, int s, int gi, float3 gr)
+{
+    if (O.attr1)
+        O.attr1[s] = make_float4(gr.x, gr.y, gr.z, 0.0f);
+    if (O.grd_out)
+        O.grd_out[gi] = make_float4(gr.x, gr.y, gr.z, 0.0f);
+}
 
 __device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, float3 n, float Ip)
 {
@@ -284,7 +340,10 @@ __device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, 
 
 // pass 1: PCA normal per grid point in FP32 -- moments about the query point,
 // closed-form eigen-system; points whose smallest eigenvalue is not separated by
-// 1e-3 of the spread are queued for the FP64 pass
+// 1e-3 of the spread are queued for the FP64 pass.  With Grad the same walk sums
+// the gradient moments (gradient_from_moments), and the gradient follows the
+// normal (for queued points, the FP64 pass computes it from the stored moments).
+template <bool Grad>
 __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n, float rn, int max_nn, NormalOut O)
 {
     const int n = *d_n;
@@ -297,10 +356,12 @@ __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n
         const float4 p4 = g.spos[s];
         const float3 p = make_float3(p4.x, p4.y, p4.z);
         const int seg = L.bseg ? (int)(g.skey[s] >> segshift) : 0;
+        const float Ip = g.sint[s];
         GridRows R;
         const bool inside = grid_rows(g, L, seg, g.gmin[seg], p, R);
         float s1x = 0, s1y = 0, s1z = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
-        int k = 0;
+        float gxx = 0, gxy = 0, gxz = 0, gyy = 0, gyz = 0, gzz = 0, mx = 0, my = 0, mz = 0;
+        int k = 0, gk = 0;
         auto acc = [&](float4 q) {
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             s1x += dx, s1y += dy, s1z += dz;
@@ -313,8 +374,18 @@ __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n
         // the two sets are the same)
         if (inside)
             grid_scan(g, R, [&](int t, float4 q) {
-                if (dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z) < rn2)
+                const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+                if (d2 < rn2)
                     acc(q);
+                if (Grad && d2 < O.grad_r2)
+                {
+                    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                    const float dI = g.sint[t] - Ip;
+                    gxx += dx * dx, gxy += dx * dy, gxz += dx * dz;
+                    gyy += dy * dy, gyz += dy * dz, gzz += dz * dz;
+                    mx += dx * dI, my += dy * dI, mz += dz * dI;
+                    ++gk;
+                }
             });
         if (inside && max_nn > 0 && k > max_nn)
         {
@@ -328,18 +399,29 @@ __global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n
         if (k >= 3)
         {
             const float ik = 1.0f / (float)k;
-            const float mx = s1x * ik, my = s1y * ik, mz = s1z * ik;
-            if (!smallest_eigvec_f32(sxx * ik - mx * mx, sxy * ik - mx * my, sxz * ik - mx * mz, syy * ik - my * my,
-                                     syz * ik - my * mz, szz * ik - mz * mz, nrm))
+            const float ux = s1x * ik, uy = s1y * ik, uz = s1z * ik;
+            if (!smallest_eigvec_f32(sxx * ik - ux * ux, sxy * ik - ux * uy, sxz * ik - ux * uz, syy * ik - uy * uy,
+                                     syz * ik - uy * uz, szz * ik - uz * uz, nrm))
             {
-                O.degen_list[atomicAdd(O.degen_count, 1)] = s;
+                const int slot = atomicAdd(O.degen_count, 1);
+                O.degen_list[slot] = s;
+                if (Grad)
+                {
+                    O.degen_mom[3 * slot] = make_float4(gxx, gxy, gxz, gyy);
+                    O.degen_mom[3 * slot + 1] = make_float4(gyz, gzz, mx, my);
+                    O.degen_mom[3 * slot + 2] = make_float4(mz, __int_as_float(gk), 0.0f, 0.0f);
+                }
                 continue; // written by the FP64 pass
             }
             // orient against (0, 0, -1) (cuda_estimate_normals.cu:131-151)
             if (nrm.z > 0.0f)
                 nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
         }
-        store_normal(O, s, g.sidx[s], nrm, g.sint[s]);
+        const int gi = g.sidx[s];
+        store_normal(O, s, gi, nrm, Ip);
+        if (Grad)
+            store_gradient(O, s, gi,
+                           gradient_from_moments(gxx, gxy, gxz, gyy, gyz, gzz, make_float3(mx, my, mz), gk, nrm));
     }
 }
 
@@ -508,7 +590,15 @@ __global__ void __launch_bounds__(128) k_normals64(GridDev g, float rn, int max_
             float3 nrm = make_float3((float)v[0], (float)v[1], (float)v[2]);
             if (nrm.z > 0.0f)
                 nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
-            store_normal(O, s, g.sidx[s], nrm, g.sint[s]);
+            const int gi = g.sidx[s];
+            store_normal(O, s, gi, nrm, g.sint[s]);
+            if (O.degen_mom)
+            {
+                const float4 m0 = O.degen_mom[3 * j], m1 = O.degen_mom[3 * j + 1], m2 = O.degen_mom[3 * j + 2];
+                store_gradient(O, s, gi,
+                               gradient_from_moments(m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, make_float3(m1.z, m1.w, m2.x),
+                                                     __float_as_int(m2.y), nrm));
+            }
         }
         __syncwarp();
     }
@@ -618,22 +708,30 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
         O.nrm_out = nrm_out;
         O.degen_count = ctx->arena.get<int>(1);
         O.degen_list = ctx->arena.get<int>(std::max<int64_t>(g.cap, 1));
-        if (!O.degen_count || !O.degen_list)
+        // the gradients in the same walk
+        O.grad_r2 = do_grad ? grad_radius * grad_radius : 0.0f;
+        O.attr1 = do_grad ? attr1 : nullptr;
+        O.grd_out = do_grad ? grd_out : nullptr;
+        O.degen_mom = do_grad ? ctx->arena.get<float4>(3 * (size_t)std::max<int64_t>(g.cap, 1)) : nullptr;
+        if (!O.degen_count || !O.degen_list || (do_grad && !O.degen_mom))
             return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "normals: scratch");
         GCA_CUDA(ctx, cudaMemsetAsync(O.degen_count, 0, sizeof(int), ctx->stream));
-        k_normals32<<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
+        if (do_grad)
+            k_normals32<true><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
+        else
+            k_normals32<false><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
         k_normals64<<<ctx->num_sms * 2, 128, 0, ctx->stream>>>(g.dev, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
     }
-    if (do_grad)
+    if (do_grad && !do_normals)
     {
         const float4 *ng = do_normals ? attr0 : nullptr;
         const float4 *no = do_normals ? (attr0 ? nullptr : nrm_out) : in_nrm;
         k_gradient<<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, grad_radius, ng, no, attr1, grd_out);
         GCA_CHECK_LAUNCH(ctx);
     }
-    else if (attr1)
+    else if (!do_grad && attr1)
         GCA_CUDA(ctx, cudaMemsetAsync(attr1, 0, sizeof(float4) * g.cap, ctx->stream));
     if (!do_normals && attr0)
     {
