@@ -21,6 +21,7 @@ namespace gca3d
 {
 
 constexpr int kFrameThreads = 256;
+constexpr int kRangeTable = 1024; // tabulated depth differences of the fixed filter
 constexpr unsigned long long kRowAgg = 1ull << 62, kRowInc = 2ull << 62, kRowFlag = 3ull << 62;
 
 
@@ -71,9 +72,25 @@ __global__ void __launch_bounds__(kFrameThreads) k_frame(const uint16_t *__restr
     __shared__ unsigned s_tile;
     __shared__ int s_wsum[kFrameThreads / 32];
     __shared__ long long s_base;
+    // the fixed filter's weights depend only on the tap offset (spatial) and on the
+    // integer depth difference (range): both tabulated once per block, the same
+    // function values as evaluating them per tap
+    __shared__ float s_wsp[(2 * kMaxFilterRadius + 1) * (2 * kMaxFilterRadius + 1)];
+    __shared__ float s_wrange[kRangeTable];
     const int R = P.mode == GCA3D_FILTER_FIXED ? P.radius : (P.mode == GCA3D_FILTER_ADAPTIVE ? 5 : 0);
     if (threadIdx.x == 0)
         s_tile = atomicAdd(tile_ctr, 1u);
+    if (P.mode == GCA3D_FILTER_FIXED)
+    {
+        const int n = 2 * R + 1;
+        for (int i = threadIdx.x; i < n * n; i += kFrameThreads)
+        {
+            const int dy = i / n - R, dx = i % n - R;
+            s_wsp[i] = gauss_sq((float)(dx * dx + dy * dy), P.sigma_space);
+        }
+        for (int d = threadIdx.x; d < kRangeTable; d += kFrameThreads)
+            s_wrange[d] = gauss((float)d, P.sigma_depth);
+    }
     __syncthreads();
     const int y = (int)s_tile;
     if (y >= P.h)
@@ -135,7 +152,12 @@ __global__ void __launch_bounds__(kFrameThreads) k_frame(const uint16_t *__restr
                         if (!nb)
                             continue;
                         const int diff = abs((int)d0 - (int)nb);
-                        const float wgt = __fmul_rn(gauss_sq((float)(dx * dx + dy * dy), ss), gauss((float)diff, sd));
+                        float wgt;
+                        if (P.mode == GCA3D_FILTER_FIXED)
+                            wgt = __fmul_rn(s_wsp[(dy + R) * (2 * R + 1) + dx + R],
+                                            diff < kRangeTable ? s_wrange[diff] : gauss((float)diff, sd));
+                        else
+                            wgt = __fmul_rn(gauss_sq((float)(dx * dx + dy * dy), ss), gauss((float)diff, sd));
                         sw = __fadd_rn(sw, wgt);
                         sum = __fadd_rn(sum, __fmul_rn(wgt, (float)nb));
                     }
