@@ -50,6 +50,8 @@ struct gca3d_icp_plan
     bool host_checks = false; // plain mode: convergence test read back after every iteration
     cudaStream_t side = nullptr; // captures the bodies of the device-side loops
     PlanPrologue prologue;       // work enqueued before the schedule (captured with it)
+    bool vox_given = false;      // voxel batches supplied by the caller
+    PlanVoxels vox;
 };
 
 namespace
@@ -101,9 +103,16 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         Batch bs, bt;
         if (S.voxel > 0.0f)
         {
+            // both clouds in Z-order of their voxels: compact source work items, and the
+            // same target whether it is downsampled here or supplied
+            if (pl->vox_given)
+            {
+                bs = pl->vox.src[si];
+                bt = pl->vox.tgt[si];
+            }
             if ((st = voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true)))
                 return st;
-            if ((st = voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt)))
+            if (!pl->vox_given && (st = voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt, true)))
                 return st;
         }
         else
@@ -307,7 +316,7 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
 
 int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
                                     const gca3d_icp_params *params, bool capture, PlanPrologue prologue,
-                                    gca3d_icp_plan **out)
+                                    gca3d_icp_plan **out, const PlanVoxels *voxels)
 {
     if (!ctx || !out || P < 1 || P > kMaxSegments || !src || !tgt)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: bad arguments (1 <= pairs <= 4096)");
@@ -330,6 +339,22 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
     pl->prm = *params;
     pl->host_checks = !params->use_graph;
     pl->prologue = std::move(prologue);
+    if (voxels)
+    {
+        for (int s = 0; s < params->n_scales; ++s)
+            if (!(params->scales[s].voxel > 0.0f))
+            {
+                delete pl;
+                return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: supplied voxel batches need a voxel size at every scale");
+            }
+        if (P != 1)
+        {
+            delete pl;
+            return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: supplied voxel batches are for one pair");
+        }
+        pl->vox_given = true;
+        pl->vox = *voxels;
+    }
     int nb = 0;
     for (int k = 0; k < P; ++k)
     {

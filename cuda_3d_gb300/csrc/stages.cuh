@@ -76,9 +76,18 @@ int frame_to_cloud(gca3d_context *ctx, const uint16_t *depth, const uint8_t *bgr
 // an ICP plan whose graph (or eager run) starts with `prologue`, enqueued on the
 // context stream with the plan's arena active (the frame stage of a tracker)
 using PlanPrologue = std::function<int(gca3d_context *)>;
+// voxel batches supplied by the caller (one pair, every scale downsampled): per
+// scale the source is downsampled into src[s] and tgt[s] is the target as it is
+// (a tracker passes the previous frame's source batches, so every frame is
+// downsampled once)
+struct PlanVoxels
+{
+    Batch src[GCA3D_MAX_SCALES];
+    Batch tgt[GCA3D_MAX_SCALES];
+};
 int icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *const *src, gca3d_cloud *const *tgt,
                              const gca3d_icp_params *params, bool capture, PlanPrologue prologue,
-                             gca3d_icp_plan **out);
+                             gca3d_icp_plan **out, const PlanVoxels *voxels = nullptr);
 
 // a single-segment batch view of a cloud (no copy; segment offsets from the arena)
 int cloud_batch(gca3d_context *ctx, gca3d_cloud *c, Batch &b);

@@ -9,11 +9,13 @@
 // buffers and two raw-cloud slots used alternately.  Frame k (k >= 1) registers
 // slot k % 2 (this frame, the source) onto slot 1 - k % 2 (the previous frame, the
 // target) with an ICP plan whose prologue uploads the staged frame and runs the
-// frame kernel into the source slot; with use_graph the whole per-frame sequence --
-// upload, filter and back-projection, voxel downsampling of both frames, target
-// normals and colour gradients, the coarse-to-fine iterations -- is one CUDA graph
-// per slot parity, replayed every frame.  The only host work per frame is the copy
-// into staging, the graph launch and the read-back of the pair state.
+// frame kernel into the source slot.  Every slot also owns one voxel batch per
+// scale: a frame is downsampled once, as the source, and its batches are the
+// target of the next frame.  With use_graph the whole per-frame sequence --
+// upload, filter and back-projection, voxel downsampling, target normals and colour
+// gradients, the coarse-to-fine iterations -- is one CUDA graph per slot parity,
+// replayed every frame.  The only host work per frame is the copy into staging,
+// the graph launch and the read-back of the pair state.
 #include "icp.cuh"
 #include "stages.cuh"
 
@@ -31,6 +33,8 @@ struct gca3d_tracker
     uint8_t *d_bgr = nullptr, *h_bgr = nullptr;
     gca3d_cloud *raw[2] = {nullptr, nullptr};
     gca3d_icp_plan *plan[2] = {nullptr, nullptr};
+    PlanVoxels vox[2];              // per slot: .src = its voxel batches per scale
+    SegSrc *d_seg[2] = {nullptr, nullptr}; // per slot: the raw cloud as a stage source
     int64_t frames = 0;
     double pose[16];
     double last[16];
@@ -84,6 +88,13 @@ int gca3d_tracker_destroy(gca3d_tracker *t)
             gca3d_icp_plan_destroy(t->plan[k]);
         if (t->raw[k])
             gca3d_cloud_destroy(t->raw[k]);
+        for (int s = 0; s < GCA3D_MAX_SCALES; ++s)
+        {
+            cudaFree(t->vox[k].src[s].pos);
+            cudaFree(t->vox[k].src[s].col);
+            cudaFree(t->vox[k].src[s].seg_off);
+        }
+        cudaFree(t->d_seg[k]);
     }
     cudaFree(t->d_depth);
     cudaFree(t->d_bgr);
@@ -128,11 +139,31 @@ int gca3d_tracker_create(gca3d_context *ctx, const gca3d_tracker_params *p, gca3
     memset(t->h_depth, 0, t->depth_bytes);
     memset(t->h_bgr, 0, t->bgr_bytes);
     for (int k = 0; k < 2; ++k)
+    {
         if ((st = gca3d_cloud_create(ctx, n, &t->raw[k])))
         {
             gca3d_tracker_destroy(t);
             return st;
         }
+        const SegSrc seg{t->raw[k]->pos, t->raw[k]->col, nullptr, t->raw[k]->d_count};
+        bool ok = cudaMalloc(&t->d_seg[k], sizeof(SegSrc)) == cudaSuccess &&
+                  cudaMemcpy(t->d_seg[k], &seg, sizeof(SegSrc), cudaMemcpyHostToDevice) == cudaSuccess;
+        for (int s = 0; ok && s < p->icp.n_scales; ++s)
+        {
+            Batch &b = t->vox[k].src[s];
+            b.P = 1;
+            b.cap = b.max_seg_cap = n;
+            ok = cudaMalloc(&b.pos, sizeof(float4) * (size_t)n) == cudaSuccess &&
+                 cudaMalloc(&b.col, sizeof(float4) * (size_t)n) == cudaSuccess &&
+                 cudaMalloc(&b.seg_off, sizeof(int32_t) * 2) == cudaSuccess;
+        }
+        if (!ok)
+        {
+            cudaGetLastError();
+            gca3d_tracker_destroy(t);
+            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "tracker: voxel batches");
+        }
+    }
     set_identity(t->pose);
     set_identity(t->last);
     *out = t;
@@ -171,6 +202,11 @@ int gca3d_tracker_push(gca3d_tracker *t, const uint16_t *depth, const uint8_t *b
         ctx->arena.reset();
         if ((st = enqueue_frame(t, t->raw[0])))
             return st;
+        // the first frame is downsampled here: it is the target of the next
+        for (int s = 0; s < t->prm.icp.n_scales; ++s)
+            if ((st = voxel_stage(ctx, t->d_seg[0], 1, t->raw[0]->capacity, t->raw[0]->capacity,
+                                  t->prm.icp.scales[s].voxel, t->vox[0].src[s], true)))
+                return st;
         GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if ((st = consume_device_error(ctx, "tracker")))
             return st;
@@ -183,9 +219,15 @@ int gca3d_tracker_push(gca3d_tracker *t, const uint16_t *depth, const uint8_t *b
         {
             gca3d_cloud *s = t->raw[cur], *g = t->raw[1 - cur];
             gca3d_cloud *src_slot = t->raw[cur];
+            PlanVoxels v;
+            for (int s2 = 0; s2 < t->prm.icp.n_scales; ++s2)
+            {
+                v.src[s2] = t->vox[cur].src[s2];
+                v.tgt[s2] = t->vox[1 - cur].src[s2];
+            }
             st = icp_plan_create_internal(
                 ctx, 1, &s, &g, &t->prm.icp, t->prm.icp.use_graph != 0,
-                [t, src_slot](gca3d_context *) { return enqueue_frame(t, src_slot); }, &t->plan[cur]);
+                [t, src_slot](gca3d_context *) { return enqueue_frame(t, src_slot); }, &t->plan[cur], &v);
             if (st)
                 return st;
         }
