@@ -127,9 +127,25 @@ __global__ void k_hash_insert(const uint64_t *skey, const int32_t *d_n, const Ke
         const unsigned long long rk = skey[s] >> bz;
         if (s > 0 && (skey[s - 1] >> bz) == rk)
             continue;
-        int e = s + 1;
-        while (e < n && (skey[e] >> bz) == rk)
-            ++e;
+        // the end of the row (the keys are sorted): galloping from s, then bisection
+        // of (lo, hi], where lo is in the row and hi is past it or n
+        int lo = s, hi = s + 1, step = 1;
+        while (hi < n && (skey[hi] >> bz) == rk)
+        {
+            lo = hi;
+            step <<= 1;
+            hi = s + step;
+        }
+        hi = min(hi, n);
+        while (hi - lo > 1)
+        {
+            const int m = (lo + hi) >> 1;
+            if ((skey[m] >> bz) == rk)
+                lo = m;
+            else
+                hi = m;
+        }
+        const int e = hi;
         uint32_t h = hash_u64(rk) & hmask;
         bool done = false;
         for (uint32_t probe = 0; probe <= hmask; ++probe)

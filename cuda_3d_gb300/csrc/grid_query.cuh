@@ -127,17 +127,18 @@ __device__ __forceinline__ NNBest nn_search_one(const GridDev &g, const KeyLayou
 // as long; the group combines its partial results with width-4 shuffles.
 // ---------------------------------------------------------------------------
 constexpr int kSub = 4;
+constexpr int kSubRows = (9 + kSub - 1) / kSub; // rows per lane
 
 struct SubRows
 {
-    int2 r[3];
+    int2 r[kSubRows];
     int lo, hi;
 };
 
 template <class F> __device__ __forceinline__ void grid_scan_sub(const GridDev &g, const SubRows &R, F &&f)
 {
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
+    for (int j = 0; j < kSubRows; ++j)
     {
         int t = R.r[j].x;
         const int e = R.r[j].y;
@@ -182,12 +183,12 @@ __device__ __forceinline__ void grid_rows_box(const GridDev &g, const KeyLayout 
     const int mx = (1 << L.bx) - 1, my = (1 << L.by) - 1;
     const unsigned long long segbits = (unsigned long long)seg << (L.bx + L.by);
     const int nrows = B.nx * B.ny;
-    unsigned long long rk[3];
-    uint32_t h[3];
-    ulonglong2 v[3];
+    unsigned long long rk[kSubRows];
+    uint32_t h[kSubRows];
+    ulonglong2 v[kSubRows];
     const uint32_t hmask = g.hmask;
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
+    for (int j = 0; j < kSubRows; ++j)
     {
         const int k = sub + kSub * j;
         const int x = B.x0 + k / B.ny, y = B.y0 + k % B.ny;
@@ -197,7 +198,7 @@ __device__ __forceinline__ void grid_rows_box(const GridDev &g, const KeyLayout 
         v[j] = ok ? slot_load(g.slots, h[j]) : make_ulonglong2(kEmptyKey, 0ull);
     }
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
+    for (int j = 0; j < kSubRows; ++j)
     {
         R.r[j] = make_int2(0, 0);
         if (rk[j] != kEmptyKey && v[j].x == rk[j])

@@ -82,36 +82,44 @@ __global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *d_
     }
 }
 
-// bucket offsets per digit, trivial-pass detection and ping-pong bookkeeping
+// bucket offsets per digit, trivial-pass detection and ping-pong bookkeeping: one
+// warp per digit, each lane scanning 8 consecutive buckets
 __global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *d_sel)
 {
-    __shared__ uint32_t s[256];
-    __shared__ int triv;
     const int n = *d_n;
-    const int t = threadIdx.x;
-    for (int d = 0; d < npasses; ++d)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = warp; d < npasses; d += blockDim.x >> 5)
     {
-        if (t == 0)
-            triv = 0;
-        uint32_t c = ctl->hist[d][t];
-        s[t] = c;
-        __syncthreads();
-        if ((int)c == n)
-            triv = 1;
-        // inclusive Hillis-Steele scan over 256 digits
-        for (int o = 1; o < 256; o <<= 1)
+        uint32_t c[8], sum = 0;
+        bool triv = n <= 1;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
         {
-            uint32_t v = t >= o ? s[t - o] : 0;
-            __syncthreads();
-            s[t] += v;
-            __syncthreads();
+            c[k] = ctl->hist[d][8 * lane + k];
+            sum += c[k];
+            triv |= (int)c[k] == n;
         }
-        ctl->off[d][t] = s[t] - c;
-        if (t == 0)
-            ctl->trivial[d] = triv || n <= 1;
-        __syncthreads();
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += y;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            ctl->off[d][8 * lane + k] = run;
+            run += c[k];
+        }
+        triv = __any_sync(0xffffffffu, triv);
+        if (lane == 0)
+            ctl->trivial[d] = triv;
     }
-    if (t == 0)
+    __syncthreads();
+    if (threadIdx.x == 0)
     {
         int sel = 0;
         for (int d = 0; d < npasses; ++d)
@@ -372,42 +380,60 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict
     if (lane == 31)
         s_wsum[warp] = x;
     __syncthreads();
-    if (threadIdx.x == 0)
+    // decoupled look-back by warp 0: the 32 nearest predecessors' states are read at
+    // once (each wait bounded), the nearest inclusive one is found by ballot and the
+    // states up to it are summed across the warp; only a window of aggregates moves
+    // the look-back 32 tiles further
+    if (warp == 0)
     {
         long long agg = 0;
         for (int w = 0; w < kScanThreads / 32; ++w)
             agg += s_wsum[w];
         unsigned long long *st = status + tile;
         long long excl = 0;
-        if (tile == 0)
-            st_release64(st, kSFlagInc | (unsigned long long)agg);
-        else
+        if (lane == 0)
+            st_release64(st, (tile == 0 ? kSFlagInc : kSFlagAgg) | (unsigned long long)agg);
+        if (tile > 0)
         {
-            st_release64(st, kSFlagAgg | (unsigned long long)agg);
-            for (int p = tile - 1; p >= 0; --p)
+            for (int top = tile - 1;; top -= 32)
             {
-                unsigned long long s = ld_acquire64(status + p);
-                uint32_t spins = 0;
-                while ((s & kSFlagMask) == 0)
+                const int p = top - lane;
+                unsigned long long s = kSFlagInc; // before tile 0: an inclusive zero
+                if (p >= 0)
                 {
-                    if (++spins > kSpinLimit)
-                    {
-                        atomicOr(d_err, kErrTimeout);
-                        break;
-                    }
-                    if (spins > 64)
-                        __nanosleep(64);
+                    uint32_t spins = 0;
                     s = ld_acquire64(status + p);
+                    while ((s & kSFlagMask) == 0)
+                    {
+                        if (++spins > kSpinLimit)
+                        {
+                            atomicOr(d_err, kErrTimeout);
+                            break;
+                        }
+                        if (spins > 64)
+                            __nanosleep(64);
+                        s = ld_acquire64(status + p);
+                    }
                 }
-                excl += (long long)(s & kSValMask);
-                if ((s & kSFlagMask) != kSFlagAgg)
+                const unsigned inc = __ballot_sync(0xffffffffu, (s & kSFlagMask) != kSFlagAgg);
+                const int stop = inc ? __ffs(inc) - 1 : 31;
+                long long v = lane <= stop ? (long long)(s & kSValMask) : 0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                excl += v;
+                if (inc)
                     break;
             }
-            st_release64(st, kSFlagInc | (unsigned long long)(excl + agg));
+            if (lane == 0)
+                st_release64(st, kSFlagInc | (unsigned long long)(excl + agg));
         }
-        s_prefix = excl;
-        if (tile == ntiles - 1 && d_total)
-            *d_total = (int32_t)(excl + agg);
+        if (lane == 0)
+        {
+            s_prefix = excl;
+            if (tile == ntiles - 1 && d_total)
+                *d_total = (int32_t)(excl + agg);
+        }
     }
     __syncthreads();
     long long run = s_prefix;
