@@ -353,20 +353,38 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restr
         continue;
     Acc<Comp> acc;
     acc.zero();
-    for (int i = b.start + threadIdx.x; i < b.end; i += kIcpThreads)
+    // a thread's points two at a time, all their loads issued before either is used
+    // (the sums still run over the points in ascending order)
+    constexpr int kPer = kIcpChunk / kIcpThreads;
+#pragma unroll
+    for (int j0 = 0; j0 < kPer; j0 += 2)
     {
-        const int2 c = corr[i];
-        if (c.x < 0)
-            continue;
-        const float4 s4 = src_pos[i];
-        const float3 p = apply_pose(s_T, s4);
-        const float4 q = __ldg(&tpos[c.x]);
-        const float4 a0 = __ldg(&attr0[c.x]);
-        const float4 a1 = __ldg(&attr1[c.x]);
-        GNTerms terms;
-        gn_terms(p, s4.w, make_float3(q.x, q.y, q.z), a0.w, make_float3(a0.x, a0.y, a0.z),
-                 make_float3(a1.x, a1.y, a1.z), slg, slc, terms);
-        acc.add_terms(terms, __int_as_float(c.y));
+        int2 c[2];
+        float4 s4[2], q[2], a0[2], a1[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+        {
+            const int i = b.start + (int)threadIdx.x + kIcpThreads * (j0 + j);
+            c[j] = i < b.end ? corr[i] : make_int2(-1, 0);
+            if (c[j].x >= 0)
+            {
+                s4[j] = src_pos[i];
+                q[j] = __ldg(&tpos[c[j].x]);
+                a0[j] = __ldg(&attr0[c[j].x]);
+                a1[j] = __ldg(&attr1[c[j].x]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+        {
+            if (c[j].x < 0)
+                continue;
+            const float3 p = apply_pose(s_T, s4[j]);
+            GNTerms terms;
+            gn_terms(p, s4[j].w, make_float3(q[j].x, q[j].y, q[j].z), a0[j].w, make_float3(a0[j].x, a0[j].y, a0[j].z),
+                     make_float3(a1[j].x, a1[j].y, a1[j].z), slg, slc, terms);
+            acc.add_terms(terms, __int_as_float(c[j].y));
+        }
     }
     block_reduce_store<Comp>(acc, partials + (size_t)w * kTermsPad);
     }
