@@ -191,7 +191,9 @@ __device__ __forceinline__ void grid_rows_box(const GridDev &g, const KeyLayout 
     for (int j = 0; j < kSubRows; ++j)
     {
         const int k = sub + kSub * j;
-        const int x = B.x0 + k / B.ny, y = B.y0 + k % B.ny;
+        // k / ny for k < 9 and ny <= 3 by a multiply: (k * ceil(256 / ny)) >> 8
+        const int kx = (k * (B.ny == 1 ? 256 : (B.ny == 2 ? 128 : 86))) >> 8;
+        const int x = B.x0 + kx, y = B.y0 + (k - kx * B.ny);
         const bool ok = k < nrows && x >= 0 && x <= mx && y >= 0 && y <= my;
         rk[j] = ok ? (segbits | ((unsigned long long)x << L.by) | (unsigned long long)y) : kEmptyKey;
         h[j] = hash_u64(rk[j]) & hmask;

@@ -247,7 +247,7 @@ __device__ __forceinline__ BlockPair item_pair(int w, const int32_t *src_off, co
 // list of the others: the search, shrunk to the cells that overlap the ball
 // through the last nearest point when that one is within max_corr (the ball holds
 // the nearest point and all its ties); it renews the point's certificate.
-__global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
+__global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                         GridDev g, const PairState *st, const int *bmap, int P,
                                                         float max_corr, int2 *corr, NNCerts cert, int32_t *nn_out,
                                                         int nn_chunk)
@@ -255,6 +255,8 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
     __shared__ int s_pair;
     __shared__ float s_T[12];
     __shared__ int s_list[kNNChunkMax];
+    __shared__ int4 s_box[kNNChunkMax]; // x0, y0, zlo, nx | ny << 8 | nz << 16 of the search box
+    __shared__ float4 s_p[kNNChunkMax]; // the transformed point
     __shared__ int s_cnt;
     const KeyLayout L = *g.layout;
     const float rr = __fmul_rn(max_corr, max_corr);
@@ -274,19 +276,42 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
     for (int base = b.start; base < b.end; base += kIcpThreads)
     {
         const int i = base + (int)threadIdx.x;
-        bool need = i < b.end;
+        bool need = false;
+        float3 p;
+        CellBox B;
+        if (i < b.end)
+        {
+            p = apply_pose(s_T, src_pos[i]);
+            need = nn_full_box(g, L, o, p, B);
+            if (!need)
+            {
+                // outside the grid's range: no candidates
+                corr[i] = make_int2(-1, __float_as_int(rr));
+                if (nn_out)
+                    nn_out[i] = -1;
+                cert.pos[i] = make_float4(p.x, p.y, p.z, 0.0f);
+                cert.t[i] = -1;
+            }
+        }
         if (need && warm)
         {
-            const float3 p = apply_pose(s_T, src_pos[i]);
-            CellBox B;
+            const int t1 = cert.t[i];
             int t;
             float d2;
-            if (nn_full_box(g, L, o, p, B) && nn_certified(g, o, p, B, cert.pos[i], cert.t[i], rr, t, d2))
+            if (nn_certified(g, o, p, B, cert.pos[i], t1, rr, t, d2))
             {
                 need = false;
                 corr[i] = make_int2(t, __float_as_int(d2));
                 if (nn_out)
                     nn_out[i] = t >= 0 ? __ldg(&g.sidx[t]) - tbase : -1;
+            }
+            else if (t1 >= 0)
+            {
+                // the ball through the last nearest point holds the nearest point and its ties
+                const float4 q = __ldg(&g.spos[t1]);
+                const float u2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
+                if (u2 < rr)
+                    nn_shrink_box(g, o, p, sqrtf(u2), B);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, need);
@@ -295,7 +320,12 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
             at = atomicAdd(&s_cnt, __popc(m));
         at = __shfl_sync(0xffffffffu, at, 0);
         if (need)
-            s_list[at + __popc(m & ((1u << lane) - 1u))] = i;
+        {
+            const int k = at + __popc(m & ((1u << lane) - 1u));
+            s_list[k] = i;
+            s_box[k] = make_int4(B.x0, B.y0, B.zlo, B.nx | (B.ny << 8) | ((B.zhi - B.zlo + 1) << 16));
+            s_p[k] = make_float4(p.x, p.y, p.z, 0.0f);
+        }
     }
     __syncthreads();
     const int n = s_cnt;
@@ -304,29 +334,20 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_nn(const float4 *__restrict
     {
         const int k = base + (int)(threadIdx.x / kSub);
         const bool valid = k < n;
-        const int i = s_list[valid ? k : 0];
-        const float3 p = apply_pose(s_T, src_pos[i]);
-        CellBox B;
-        const bool in = nn_full_box(g, L, o, p, B);
-        if (warm && valid && in)
-        {
-            const int t = cert.t[i];
-            if (t >= 0)
-            {
-                const float4 q = __ldg(&g.spos[t]);
-                const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
-                if (d2 < rr)
-                    nn_shrink_box(g, o, p, sqrtf(d2), B);
-            }
-        }
-        const NNBest2 best = nn_search_box2(g, L, b.pair, B, p, valid && in);
+        const int kk = valid ? k : 0;
+        const int i = s_list[kk];
+        const int4 bx = s_box[kk];
+        const float4 p4 = s_p[kk];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
+        const CellBox B{bx.x, bx.w & 0xff, bx.y, (bx.w >> 8) & 0xff, bx.z, bx.z + (bx.w >> 16) - 1};
+        const NNBest2 best = nn_search_box2(g, L, b.pair, B, p, valid);
         if (valid && (threadIdx.x & (kSub - 1)) == 0)
         {
             const bool hit = best.t >= 0 && best.d2 < rr;
             corr[i] = make_int2(hit ? best.t : -1, __float_as_int(hit ? best.d2 : rr));
             if (nn_out)
                 nn_out[i] = hit ? __ldg(&g.sidx[best.t]) - tbase : -1;
-            cert.pos[i] = make_float4(p.x, p.y, p.z, in ? cert_bound(g, o, p, B, best.s2) : 0.0f);
+            cert.pos[i] = make_float4(p.x, p.y, p.z, cert_bound(g, o, p, B, best.s2));
             cert.t[i] = best.t;
         }
     }
