@@ -553,22 +553,46 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
     s_sum[threadIdx.x] = a;
     s_sum_nn[threadIdx.x] = an;
     __syncthreads();
-    if (threadIdx.x == 0)
+    if (threadIdx.x < 32)
     {
-        int x = 0, y = 0;
-        for (int k = 0; k < kIcpThreads; ++k)
+        // exclusive prefix of the 256 per-thread sums: 8 per lane, then across the warp
+        const int l = threadIdx.x;
+        int va[kIcpThreads / 32], vn[kIcpThreads / 32], sa = 0, sn = 0;
+#pragma unroll
+        for (int k = 0; k < kIcpThreads / 32; ++k)
         {
-            const int u = s_sum[k], v = s_sum_nn[k];
-            s_sum[k] = x, s_sum_nn[k] = y;
-            x += u, y += v;
+            va[k] = s_sum[l * (kIcpThreads / 32) + k];
+            vn[k] = s_sum_nn[l * (kIcpThreads / 32) + k];
+            sa += va[k];
+            sn += vn[k];
         }
-        bmap[P] = x;
-        bmap_nn[P] = y;
-        *loop.ticket = 0u;
-        if (loop.iter)
+        int ia = sa, in = sn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
         {
-            const int it = ++(*loop.iter);
-            cudaGraphSetConditional(loop.handle, (y > 0 && it < loop.max_iter) ? 1u : 0u);
+            const int ya = __shfl_up_sync(0xffffffffu, ia, o), yn = __shfl_up_sync(0xffffffffu, in, o);
+            if (l >= o)
+                ia += ya, in += yn;
+        }
+        int ra = ia - sa, rn = in - sn;
+#pragma unroll
+        for (int k = 0; k < kIcpThreads / 32; ++k)
+        {
+            s_sum[l * (kIcpThreads / 32) + k] = ra;
+            s_sum_nn[l * (kIcpThreads / 32) + k] = rn;
+            ra += va[k];
+            rn += vn[k];
+        }
+        if (l == 31)
+        {
+            bmap[P] = ra;
+            bmap_nn[P] = rn;
+            *loop.ticket = 0u;
+            if (loop.iter)
+            {
+                const int it = ++(*loop.iter);
+                cudaGraphSetConditional(loop.handle, (rn > 0 && it < loop.max_iter) ? 1u : 0u);
+            }
         }
     }
     __syncthreads();

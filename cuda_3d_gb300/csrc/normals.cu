@@ -344,7 +344,7 @@ __device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, 
 // the gradient moments (gradient_from_moments), and the gradient follows the
 // normal (for queued points, the FP64 pass computes it from the stored moments).
 template <bool Grad>
-__global__ void __launch_bounds__(256) k_normals32(GridDev g, const int32_t *d_n, float rn, int max_nn, NormalOut O)
+__global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *d_n, float rn, int max_nn, NormalOut O)
 {
     const int n = *d_n;
     const KeyLayout L = *g.layout;
