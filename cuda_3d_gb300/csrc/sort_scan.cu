@@ -18,6 +18,7 @@ constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems; // 2048 keys per tile
 constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kLookWindow = 8; // predecessor tiles read at once in the look-back
 
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
@@ -41,6 +42,14 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
 {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+// a state word holds its flag and its count together, so a reader that uses only
+// the word itself needs no ordering: relaxed loads, several in flight at once
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p)
+{
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 __device__ __forceinline__ void st_release64(unsigned long long *p, unsigned long long v)
@@ -132,7 +141,7 @@ __global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *
     }
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_sort_pass(
+__global__ void __launch_bounds__(kSortThreads, 5) k_sort_pass(
     uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, uint32_t *status,
     uint32_t *status_next, int64_t status_words, int pass, const int32_t *d_n, int *d_err)
 {
@@ -229,27 +238,36 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
     else
     {
         st_release(st, kFlagAgg | tot);
-        int64_t p = (int64_t)tile - 1;
-        while (p >= 0)
+        // the predecessors' states for this digit, kLookWindow at a time (independent
+        // relaxed loads), consumed nearest first up to the nearest inclusive one
+        bool found = false;
+        for (int64_t p = (int64_t)tile - 1; p >= 0 && !found; p -= kLookWindow)
         {
-            const uint32_t *ps = status + p * 256 + t;
-            uint32_t s = ld_acquire(ps);
-            uint32_t spins = 0;
-            while ((s & kFlagMask) == 0)
+            uint32_t s[kLookWindow];
+#pragma unroll
+            for (int j = 0; j < kLookWindow; ++j)
+                s[j] = p - j >= 0 ? ld_relaxed(status + (p - j) * 256 + t) : kFlagInc;
+#pragma unroll
+            for (int j = 0; j < kLookWindow; ++j)
             {
-                if (++spins > kSpinLimit)
-                {
-                    atomicOr(d_err, kErrTimeout);
+                if (found)
                     break;
+                uint32_t spins = 0;
+                while ((s[j] & kFlagMask) == 0)
+                {
+                    if (++spins > kSpinLimit)
+                    {
+                        atomicOr(d_err, kErrTimeout);
+                        break;
+                    }
+                    if (spins > 64)
+                        __nanosleep(64);
+                    s[j] = ld_relaxed(status + (p - j) * 256 + t);
                 }
-                if (spins > 64)
-                    __nanosleep(64);
-                s = ld_acquire(ps);
+                excl += s[j] & kCountMask;
+                if ((s[j] & kFlagMask) != kFlagAgg)
+                    found = true;
             }
-            excl += s & kCountMask;
-            if ((s & kFlagMask) != kFlagAgg)
-                break;
-            --p;
         }
         st_release(st, kFlagInc | (excl + tot));
     }
@@ -298,6 +316,10 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_pass(
 int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t cap, int max_bits,
                const int * /*d_key_bits*/)
 {
+    // five resident tiles per SM need the shared-memory side of the L1 carveout
+    static const bool carveout = cudaFuncSetAttribute(k_sort_pass, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                      cudaSharedmemCarveoutMaxShared) == cudaSuccess;
+    (void)carveout;
     const int npasses = max_bits <= 0 ? 1 : (max_bits + 7) / 8;
     const int64_t ntiles = (cap + kSortTile - 1) / kSortTile;
     const int64_t status_words = (ntiles > 0 ? ntiles : 1) * 256;
