@@ -67,6 +67,9 @@ def parse_args(argv=None):
                    "single pair, adjoint, stream)")
     p.add_argument("--no-tune", action="store_true", help="default launch shape instead of the autotuner's")
     p.add_argument("--stream-frames", type=int, default=200, help="frames of the 640x480 stream (720p: half)")
+    p.add_argument("--frame-pair", type=int, default=0, metavar="PUSHES",
+                   help="only the 640x480 frame pair: PUSHES alternating tracker pushes (graph mode, or eager "
+                        "with --eager), one JSON line")
     return p.parse_args(argv)
 
 
@@ -566,10 +569,29 @@ def run_reference(args):
     }))
 
 
+def run_frame_pair(args):
+    """the 640x480 frame pair alone (the per-row measurement of run_rows), e.g. under a
+    profiler: the two views alternate through one tracker, every push registers one pair"""
+    from cuda_3d_gb300 import build, native as N
+    from cuda_3d_gb300 import synth
+
+    build.build()
+    ctx = N.Context(0)
+    fp = synth.frame_pair(seed=0)
+    seq = [(fp.depth0, fp.bgr0), (fp.depth1, fp.bgr1)] * ((args.frame_pair + 1) // 2)
+    # --eager: launched eagerly with host convergence checks (what a profiler can follow)
+    lat, res, _, kern = _track(N, ctx, fp.cam, seq[:args.frame_pair], not args.eager, True, constant_velocity=False)
+    steady = lat[4:] if len(lat) > 6 else lat[1:]
+    print(json.dumps({"metric": "640x480 frame pair (ms, host buffers in, pose out)", "pushes": len(lat),
+                      **_lat(steady), "iterations": res[-1]["iterations"], "kernels_per_push": kern}))
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         run_reference(args)
+    elif args.frame_pair:
+        run_frame_pair(args)
     else:
         run_ours(args)
 
