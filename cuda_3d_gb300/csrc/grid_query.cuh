@@ -135,6 +135,39 @@ struct SubRows
     int lo, hi;
 };
 
+// a position in [t, e] at most 8 before the first one whose z cell is >= lo (the
+// row is sorted by z cell): a 4-way search, its three probes loaded together
+__device__ __forceinline__ int row_seek_z(const int *scz, int t, int e, int lo)
+{
+    int a = t, n = e - t; // the first z cell >= lo is in [a, a + n]
+    while (n > 8)
+    {
+        const int s = n >> 2;
+        const int c1 = __ldg(&scz[a + s]), c2 = __ldg(&scz[a + 2 * s]), c3 = __ldg(&scz[a + 3 * s]);
+        if (c3 < lo)
+        {
+            a += 3 * s + 1;
+            n -= 3 * s + 1;
+        }
+        else if (c2 < lo)
+        {
+            a += 2 * s + 1;
+            n = s - 1;
+        }
+        else if (c1 < lo)
+        {
+            a += s + 1;
+            n = s - 1;
+        }
+        else
+            n = s;
+    }
+    return a;
+}
+
+// scan the rows in order; a lane reads kScanBatch candidates at a time, so their
+// loads overlap instead of each waiting for the test of the one before
+constexpr int kScanBatch = 4;
 template <class F> __device__ __forceinline__ void grid_scan_sub(const GridDev &g, const SubRows &R, F &&f)
 {
 #pragma unroll
@@ -145,27 +178,21 @@ template <class F> __device__ __forceinline__ void grid_scan_sub(const GridDev &
         if (t >= e)
             continue;
         if (e - t > 8)
+            t = row_seek_z(g.scz, t, e, R.lo);
+        for (bool more = true; more && t < e; t += kScanBatch)
         {
-            int a = t, b = e;
-            while (a < b)
+            float4 q[kScanBatch];
+#pragma unroll
+            for (int u = 0; u < kScanBatch; ++u)
+                q[u] = t + u < e ? __ldg(&g.spos[t + u]) : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7fffffff));
+#pragma unroll
+            for (int u = 0; u < kScanBatch; ++u)
             {
-                const int m = (a + b) >> 1;
-                if (__ldg(&g.scz[m]) < R.lo)
-                    a = m + 1;
-                else
-                    b = m;
+                const int qz = __float_as_int(q[u].w);
+                more = more && qz <= R.hi;
+                if (more && qz >= R.lo)
+                    f(t + u, q[u]);
             }
-            t = a;
-        }
-        for (; t < e; ++t)
-        {
-            const float4 q = __ldg(&g.spos[t]);
-            const int qz = __float_as_int(q.w);
-            if (qz < R.lo)
-                continue;
-            if (qz > R.hi)
-                break;
-            f(t, q);
         }
     }
 }
