@@ -189,6 +189,7 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
     }
     bmap[P] = b;
     bmap_nn[P] = bn;
+    bmap_nn[P + 1] = 0; // the correspondence kernel's work queue
 }
 
 __global__ void k_state_init(PairState *st, int P, const double *T_init)
@@ -250,9 +251,9 @@ __device__ __forceinline__ BlockPair item_pair(int w, const int32_t *src_off, co
 __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                         GridDev g, const PairState *st, const int *bmap, int P,
                                                         float max_corr, int2 *corr, NNCerts cert, int32_t *nn_out,
-                                                        int nn_chunk)
+                                                        int nn_chunk, int *queue)
 {
-    __shared__ int s_pair;
+    __shared__ int s_pair, s_w;
     __shared__ float s_T[12];
     __shared__ int s_list[kNNChunkMax];
     __shared__ int4 s_box[kNNChunkMax]; // x0, y0, zlo, nx | ny << 8 | nz << 16 of the search box
@@ -262,8 +263,18 @@ __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restr
     const float rr = __fmul_rn(max_corr, max_corr);
     const int items = bmap[P];
     const int lane = threadIdx.x & 31;
-    for (int w = blockIdx.x; w < items; w += gridDim.x)
+    for (int first = 1;; first = 0)
     {
+    // a block's first work item is its own index, the later ones come from the
+    // iteration's queue: blocks that draw quick items (mostly certified points) take
+    // more of them
+    __syncthreads();
+    if (threadIdx.x == 0)
+        s_w = first ? (int)blockIdx.x : (int)gridDim.x + atomicAdd(queue, 1);
+    __syncthreads();
+    const int w = s_w;
+    if (w >= items)
+        break;
     const BlockPair b = item_pair(w, src_off, st, bmap, P, nn_chunk, s_T, &s_pair);
     if (b.pair < 0)
         continue;
@@ -587,6 +598,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
         {
             bmap[P] = ra;
             bmap_nn[P] = rn;
+            bmap_nn[P + 1] = 0;
             *loop.ticket = 0u;
             if (loop.iter)
             {
@@ -650,7 +662,7 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
     const int grid_acc = std::max(std::min(max_blocks, ctx->num_sms * shape.acc_bps), 1);
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
     k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
-                                                       corr, cert, nn_out, shape.nn_chunk);
+                                                       corr, cert, nn_out, shape.nn_chunk, bmap_nn + src.P + 1);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
         k_icp_accum<true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,

@@ -145,7 +145,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         const NNCerts cert{ctx->arena.get<float4>(std::max<int64_t>(bs.cap, 1)),
                            ctx->arena.get<int>(std::max<int64_t>(bs.cap, 1))};
         int *bmap = ctx->arena.get<int>(P + 1);
-        int *bmap_nn = ctx->arena.get<int>(P + 1);
+        int *bmap_nn = ctx->arena.get<int>(P + 2); // offsets, total, work queue
         float4 *nrm_b = own_nn_grid && !keep ? ctx->arena.get<float4>(g.cap) : nullptr;
         float4 *grd_b = own_nn_grid ? ctx->arena.get<float4>(g.cap) : nullptr;
         if (!attr0 || !attr1 || !partials || !corr || !cert.pos || !cert.t || !bmap || !bmap_nn || (own_nn_grid && (!grd_b || (!keep && !nrm_b))))
