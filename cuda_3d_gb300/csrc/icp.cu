@@ -346,19 +346,30 @@ __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restr
         const int k = base + (int)(threadIdx.x / kSub);
         const bool valid = k < n;
         const int kk = valid ? k : 0;
-        const int i = s_list[kk];
-        const int4 bx = s_box[kk];
-        const float4 p4 = s_p[kk];
-        const float3 p = make_float3(p4.x, p4.y, p4.z);
-        const CellBox B{bx.x, bx.w & 0xff, bx.y, (bx.w >> 8) & 0xff, bx.z, bx.z + (bx.w >> 16) - 1};
-        const NNBest2 best = nn_search_box2(g, L, b.pair, B, p, valid);
+        NNBest2 best;
+        {
+            const int4 bx = s_box[kk];
+            const float4 p4 = s_p[kk];
+            const CellBox B{bx.x, bx.w & 0xff, bx.y, (bx.w >> 8) & 0xff, bx.z, bx.z + (bx.w >> 16) - 1};
+            best = nn_search_box2(g, L, b.pair, B, make_float3(p4.x, p4.y, p4.z), valid);
+        }
         if (valid && (threadIdx.x & (kSub - 1)) == 0)
         {
+            // the point, its box and the grid origin read again (volatile: not kept
+            // live in registers through the search)
+            const volatile int *vl = s_list;
+            const volatile int *vb = reinterpret_cast<const volatile int *>(&s_box[kk]);
+            const volatile float *vp = reinterpret_cast<const volatile float *>(&s_p[kk]);
+            const int i = vl[kk];
+            const int bw = vb[3];
+            const CellBox B{vb[0], bw & 0xff, vb[1], (bw >> 8) & 0xff, vb[2], vb[2] + (bw >> 16) - 1};
+            const float3 p = make_float3(vp[0], vp[1], vp[2]);
+            const float3 og = g.gmin[b.pair];
             const bool hit = best.t >= 0 && best.d2 < rr;
             corr[i] = make_int2(hit ? best.t : -1, __float_as_int(hit ? best.d2 : rr));
             if (nn_out)
                 nn_out[i] = hit ? __ldg(&g.sidx[best.t]) - tbase : -1;
-            cert.pos[i] = make_float4(p.x, p.y, p.z, cert_bound(g, o, p, B, best.s2));
+            cert.pos[i] = make_float4(p.x, p.y, p.z, cert_bound(g, og, p, B, best.s2));
             cert.t[i] = best.t;
         }
     }
