@@ -53,42 +53,71 @@ __device__ __forceinline__ bool grid_rows(const GridDev &g, const KeyLayout &L, 
     return true;
 }
 
+// a position in [t, e] at most 8 before the first one whose z cell is >= lo (the
+// row is sorted by z cell): a 4-way search, its three probes loaded together
+__device__ __forceinline__ int row_seek_z(const int *scz, int t, int e, int lo)
+{
+    int a = t, n = e - t; // the first z cell >= lo is in [a, a + n]
+    while (n > 8)
+    {
+        const int s = n >> 2;
+        const int c1 = __ldg(&scz[a + s]), c2 = __ldg(&scz[a + 2 * s]), c3 = __ldg(&scz[a + 3 * s]);
+        if (c3 < lo)
+        {
+            a += 3 * s + 1;
+            n -= 3 * s + 1;
+        }
+        else if (c2 < lo)
+        {
+            a += 2 * s + 1;
+            n = s - 1;
+        }
+        else if (c1 < lo)
+        {
+            a += s + 1;
+            n = s - 1;
+        }
+        else
+            n = s;
+    }
+    return a;
+}
+
+// visit the points of row [t, e) whose z cell lies in [lo, hi] in order, reading
+// Batch candidates per load round (their loads overlap instead of each waiting for
+// the test of the one before).  f(t, spos[t]).
+template <int Batch, class F>
+__device__ __forceinline__ void row_scan(const GridDev &g, int t, int e, int lo, int hi, F &&f)
+{
+    if (t >= e)
+        return;
+    if (e - t > 8)
+        t = row_seek_z(g.scz, t, e, lo);
+    for (bool more = true; more && t < e; t += Batch)
+    {
+        float4 q[Batch];
+#pragma unroll
+        for (int u = 0; u < Batch; ++u)
+            q[u] = t + u < e ? __ldg(&g.spos[t + u]) : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7fffffff));
+#pragma unroll
+        for (int u = 0; u < Batch; ++u)
+        {
+            const int qz = __float_as_int(q[u].w);
+            more = more && qz <= hi;
+            if (more && qz >= lo)
+                f(t + u, q[u]);
+        }
+    }
+}
+
 // visit the points of the probed rows whose z cell lies in [lo, hi], in the
 // reference's scan order (x offset, then y offset, then z, then ascending original
 // index; nn_search_functor, src/geometry/cuda_nn_search.cu:164-206).  f(t, spos[t]).
-template <class F> __device__ __forceinline__ void grid_scan(const GridDev &g, const GridRows &R, F &&f)
+template <int Batch = 1, class F> __device__ __forceinline__ void grid_scan(const GridDev &g, const GridRows &R, F &&f)
 {
 #pragma unroll
     for (int k = 0; k < 9; ++k)
-    {
-        int t = R.r[k].x;
-        const int e = R.r[k].y;
-        if (t >= e)
-            continue;
-        if (e - t > 16)
-        {
-            int a = t, b = e;
-            while (a < b)
-            {
-                const int m = (a + b) >> 1;
-                if (__ldg(&g.scz[m]) < R.lo)
-                    a = m + 1;
-                else
-                    b = m;
-            }
-            t = a;
-        }
-        for (; t < e; ++t)
-        {
-            const float4 q = __ldg(&g.spos[t]);
-            const int qz = __float_as_int(q.w);
-            if (qz < R.lo)
-                continue;
-            if (qz > R.hi)
-                break;
-            f(t, q);
-        }
-    }
+        row_scan<Batch>(g, R.r[k].x, R.r[k].y, R.lo, R.hi, f);
 }
 
 template <class F>
@@ -135,66 +164,13 @@ struct SubRows
     int lo, hi;
 };
 
-// a position in [t, e] at most 8 before the first one whose z cell is >= lo (the
-// row is sorted by z cell): a 4-way search, its three probes loaded together
-__device__ __forceinline__ int row_seek_z(const int *scz, int t, int e, int lo)
-{
-    int a = t, n = e - t; // the first z cell >= lo is in [a, a + n]
-    while (n > 8)
-    {
-        const int s = n >> 2;
-        const int c1 = __ldg(&scz[a + s]), c2 = __ldg(&scz[a + 2 * s]), c3 = __ldg(&scz[a + 3 * s]);
-        if (c3 < lo)
-        {
-            a += 3 * s + 1;
-            n -= 3 * s + 1;
-        }
-        else if (c2 < lo)
-        {
-            a += 2 * s + 1;
-            n = s - 1;
-        }
-        else if (c1 < lo)
-        {
-            a += s + 1;
-            n = s - 1;
-        }
-        else
-            n = s;
-    }
-    return a;
-}
-
-// scan the rows in order; a lane reads kScanBatch candidates at a time, so their
-// loads overlap instead of each waiting for the test of the one before
+// scan the rows in order, kScanBatch candidates per load round
 constexpr int kScanBatch = 4;
 template <class F> __device__ __forceinline__ void grid_scan_sub(const GridDev &g, const SubRows &R, F &&f)
 {
 #pragma unroll
     for (int j = 0; j < kSubRows; ++j)
-    {
-        int t = R.r[j].x;
-        const int e = R.r[j].y;
-        if (t >= e)
-            continue;
-        if (e - t > 8)
-            t = row_seek_z(g.scz, t, e, R.lo);
-        for (bool more = true; more && t < e; t += kScanBatch)
-        {
-            float4 q[kScanBatch];
-#pragma unroll
-            for (int u = 0; u < kScanBatch; ++u)
-                q[u] = t + u < e ? __ldg(&g.spos[t + u]) : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(0x7fffffff));
-#pragma unroll
-            for (int u = 0; u < kScanBatch; ++u)
-            {
-                const int qz = __float_as_int(q[u].w);
-                more = more && qz <= R.hi;
-                if (more && qz >= R.lo)
-                    f(t + u, q[u]);
-            }
-        }
-    }
+        row_scan<kScanBatch>(g, R.r[j].x, R.r[j].y, R.lo, R.hi, f);
 }
 
 // the cells [x0, x0 + nx) x [y0, y0 + ny) x [zlo, zhi] of a search

@@ -343,6 +343,11 @@ __device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, 
 // 1e-3 of the spread are queued for the FP64 pass.  With Grad the same walk sums
 // the gradient moments (gradient_from_moments), and the gradient follows the
 // normal (for queued points, the FP64 pass computes it from the stored moments).
+// candidates a thread reads per load round in its row walk: one, because the 19
+// moment sums already fill the registers (wider rounds spill on the multi-scale
+// batches)
+constexpr int kNormScanBatch = 1;
+
 template <bool Grad>
 __global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *d_n, float rn, int max_nn, NormalOut O)
 {
@@ -373,7 +378,7 @@ __global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *
         // are the max_nn nearest selected instead (most points have fewer, and then
         // the two sets are the same)
         if (inside)
-            grid_scan(g, R, [&](int t, float4 q) {
+            grid_scan<kNormScanBatch>(g, R, [&](int t, float4 q) {
                 const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
                 if (d2 < rn2)
                     acc(q);

@@ -228,16 +228,44 @@ __global__ void __launch_bounds__(kSortThreads, 5) k_sort_pass(
         s_whist[w][t] = tot;
         tot += c;
     }
+    // this tile's count of digit t, published for the tiles after it
+    uint32_t *st = status + (int64_t)tile * 256 + t;
+    st_release(st, (tile == 0 ? kFlagInc : kFlagAgg) | tot);
+    // exclusive scan of the tile totals over digits (block scan of 256 values)
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int w = 0; w < warp; ++w)
+        wpre += s_wsum[w];
+    const uint32_t tile_excl = wpre + x - tot;
+    s_excl[t] = tile_excl;
+    __syncthreads();
+    // stage in tile-sorted order (needs only this tile's counts), so the keys leave
+    // the registers before the look-back
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        if (base + it * 32 + lane < n)
+        {
+            const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
+            const uint32_t pl = s_excl[d] + s_whist[warp][d] + rank[it];
+            s_keys[pl] = k[it];
+            s_vals[pl] = v[it];
+        }
+    }
     // decoupled look-back across tiles for digit t
     uint32_t excl = 0;
-    uint32_t *st = status + (int64_t)tile * 256 + t;
-    if (tile == 0)
+    if (tile > 0)
     {
-        st_release(st, kFlagInc | tot);
-    }
-    else
-    {
-        st_release(st, kFlagAgg | tot);
         // the predecessors' states for this digit, kLookWindow at a time (independent
         // relaxed loads), consumed nearest first up to the nearest inclusive one
         bool found = false;
@@ -271,36 +299,7 @@ __global__ void __launch_bounds__(kSortThreads, 5) k_sort_pass(
         }
         st_release(st, kFlagInc | (excl + tot));
     }
-    // exclusive scan of the tile totals over digits (block scan of 256 values)
-    uint32_t x = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o)
-            x += y;
-    }
-    if (lane == 31)
-        s_wsum[warp] = x;
-    __syncthreads();
-    uint32_t wpre = 0;
-    for (int w = 0; w < warp; ++w)
-        wpre += s_wsum[w];
-    const uint32_t tile_excl = wpre + x - tot;
-    s_excl[t] = tile_excl;
     s_gbase[t] = ctl->off[pass][t] + excl - tile_excl;
-    __syncthreads();
-    // stage in tile-sorted order
-#pragma unroll
-    for (int it = 0; it < kSortItems; ++it)
-    {
-        if (dig[it] < 256u)
-        {
-            uint32_t pl = s_excl[dig[it]] + s_whist[warp][dig[it]] + rank[it];
-            s_keys[pl] = k[it];
-            s_vals[pl] = v[it];
-        }
-    }
     __syncthreads();
     const int cnt = min(kSortTile, n - (int)tile * kSortTile);
     for (int j = threadIdx.x; j < cnt; j += kSortThreads)
