@@ -452,17 +452,31 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
         const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
         if (lane < kTerms)
         {
-            double v = 0.0;
-            float vf = 0.0f;
-            for (int j = grp; j < nb; j += kIcpThreads / 32)
+            constexpr int kW = kIcpThreads / 32;
+            const double *src = partials + (size_t)bstart * kTermsPad + lane;
+            if (Comp)
             {
-                const double x = partials[(size_t)(bstart + j) * kTermsPad + lane];
-                if (Comp)
-                    v += x;
-                else
-                    vf += (float)x;
+                // four running sums (blocks grp + 8 (4 q + r), r = 0..3), added in a fixed order
+                double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+                int j = grp;
+                for (; j + 3 * kW < nb; j += 4 * kW)
+                {
+                    v0 += src[(size_t)j * kTermsPad];
+                    v1 += src[(size_t)(j + kW) * kTermsPad];
+                    v2 += src[(size_t)(j + 2 * kW) * kTermsPad];
+                    v3 += src[(size_t)(j + 3 * kW) * kTermsPad];
+                }
+                for (; j < nb; j += kW)
+                    v0 += src[(size_t)j * kTermsPad];
+                s_red[grp][lane] = (v0 + v1) + (v2 + v3);
             }
-            s_red[grp][lane] = Comp ? v : (double)vf;
+            else
+            {
+                float vf = 0.0f;
+                for (int j = grp; j < nb; j += kW)
+                    vf += (float)src[(size_t)j * kTermsPad];
+                s_red[grp][lane] = (double)vf;
+            }
         }
         __syncthreads();
         __shared__ double s_S[kTermsPad];
@@ -555,10 +569,15 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
     // the last block: work maps over the pairs still active (the next iteration's
     // NN and accumulate launches get no items for converged pairs) and, in a
     // captured schedule, the loop condition
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0)
-        s_last = atomicAdd(loop.ticket, 1u) == gridDim.x - 1;
+    if (gridDim.x > 1)
+    {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_last = atomicAdd(loop.ticket, 1u) == gridDim.x - 1;
+    }
+    else if (threadIdx.x == 0)
+        s_last = 1; // one pair: this block is the last, and its own writes are visible after the barrier
     __syncthreads();
     if (!s_last)
         return;

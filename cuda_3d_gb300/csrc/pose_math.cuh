@@ -173,8 +173,77 @@ __device__ inline int solve6_device(const double *S /* 21 upper + 6 rhs */, doub
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int tri_lane(int i, int j) { return i * (i + 1) / 2 + j; } // i >= j
 
+// Short FP64 chains for the warp-parallel solve and step map, where each dependent
+// FP64 operation costs tens of nanoseconds.
+//
+// rcp_nr: 1/d by Newton-Raphson, two steps (e = 1 - d r, r += r e; each step squares
+// the relative error) from the approximate reciprocal rcp.approx.ftz.f64 (about
+// 2^-20).  Within one unit in the last place of 1/d for normal d whose reciprocal
+// is normal (0 for a reciprocal below the normal range); half the latency of the
+// IEEE division.
+__device__ __forceinline__ double rcp_nr(double d)
+{
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+    double e = fma(-d, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-d, r, 1.0);
+    return fma(r, e, r);
+}
+
+// sin x and cos x for |x| <= kSmallAngle from their Taylor series (Horner in x^2,
+// through x^13 and x^14; the first omitted terms are below 1e-18 relative)
+constexpr double kSmallAngle = 0.25;
+__device__ __forceinline__ void sincos_small(double x, double &s, double &c)
+{
+    const double z = x * x;
+    double ps = 1.0 / 6227020800.0; // 1/13!
+    double pc = 1.0 / 87178291200.0; // 1/14!
+    ps = fma(ps, -z, 1.0 / 39916800.0);
+    pc = fma(pc, -z, 1.0 / 479001600.0);
+    ps = fma(ps, -z, 1.0 / 362880.0);
+    pc = fma(pc, -z, 1.0 / 3628800.0);
+    ps = fma(ps, -z, 1.0 / 5040.0);
+    pc = fma(pc, -z, 1.0 / 40320.0);
+    ps = fma(ps, -z, 1.0 / 120.0);
+    pc = fma(pc, -z, 1.0 / 720.0);
+    ps = fma(ps, -z, 1.0 / 6.0);
+    pc = fma(pc, -z, 1.0 / 24.0);
+    pc = fma(pc, -z, 0.5);
+    s = fma(-x * z, ps, x);
+    c = fma(-z, pc, 1.0);
+}
+
+// the coefficients of the SO(3) / SE(3) exponential, A = sin t / t,
+// B = (1 - cos t) / t^2, C = (t - sin t) / t^3, as series in t2 = t^2 for
+// t2 <= kSmallAngle^2 (A = sum (-t2)^n / (2n+1)!, B = sum (-t2)^n / (2n+2)!,
+// C = sum (-t2)^n / (2n+3)!, n <= 6; the first omitted terms are below 1e-19)
+__device__ __forceinline__ void exp_coeffs_small(double t2, double &A, double &B, double &C)
+{
+    double a = 1.0 / 6227020800.0, b = 1.0 / 87178291200.0, c = 1.0 / 1307674368000.0; // 1/13!, 1/14!, 1/15!
+    a = fma(a, -t2, 1.0 / 39916800.0);
+    b = fma(b, -t2, 1.0 / 479001600.0);
+    c = fma(c, -t2, 1.0 / 6227020800.0);
+    a = fma(a, -t2, 1.0 / 362880.0);
+    b = fma(b, -t2, 1.0 / 3628800.0);
+    c = fma(c, -t2, 1.0 / 39916800.0);
+    a = fma(a, -t2, 1.0 / 5040.0);
+    b = fma(b, -t2, 1.0 / 40320.0);
+    c = fma(c, -t2, 1.0 / 362880.0);
+    a = fma(a, -t2, 1.0 / 120.0);
+    b = fma(b, -t2, 1.0 / 720.0);
+    c = fma(c, -t2, 1.0 / 5040.0);
+    a = fma(a, -t2, 1.0 / 6.0);
+    b = fma(b, -t2, 1.0 / 24.0);
+    c = fma(c, -t2, 1.0 / 120.0);
+    A = fma(a, -t2, 1.0);
+    B = fma(b, -t2, 0.5);
+    C = fma(c, -t2, 1.0 / 6.0);
+}
+
 // solve6_device over one warp (same symmetric pivots, factorisation and
-// substitutions; the backward substitution sums in the opposite order).  Lane
+// substitutions; the backward substitution sums in the opposite order, and the
+// reciprocals of the pivots are rcp_nr's).  Lane
 // tri_lane(i, j) < 21 holds A[i][j] of the lower triangle, lanes 21..26 the
 // right-hand side.  All 32 lanes call it; every lane returns the status and x.
 __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double x[6])
@@ -236,7 +305,7 @@ __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double
         }
         else
         {
-            const double inv = 1.0 / Dk; // one reciprocal per pivot, as solve6_device
+            const double inv = rcp_nr(Dk); // one reciprocal per pivot
             if (lcol)
                 a *= inv;
             const bool upd = mat && lj > k;
@@ -258,7 +327,7 @@ __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double
             acc -= lij * yj;
     }
     if (diag)
-        acc = fabs(a) > kTiny ? acc / a : 0.0;
+        acc = fabs(a) > kTiny ? acc * rcp_nr(a) : 0.0;
     // L^T z = y, by columns from the last
 #pragma unroll
     for (int j = 5; j > 0; --j)
@@ -283,9 +352,10 @@ __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double
 }
 
 // pose_from_x_device over one warp: every lane returns Ti[lane] for lane < 16
-// (row-major 4x4), the same formulas with the three sines and cosines of the
-// Euler map (or the coefficient divisions of the exponential) on separate lanes
-// and one matrix entry per lane.
+// (row-major 4x4), the same formulas with one matrix entry per lane.  The three
+// sines and cosines of the Euler map are on separate lanes (sincos_small up to
+// kSmallAngle); the exponential's coefficients are exp_coeffs_small's series up to
+// a rotation of kSmallAngle, else three divisions on separate lanes.
 __device__ inline double pose_from_x_warp(const double x[6], int map)
 {
     const unsigned full = 0xffffffffu;
@@ -298,7 +368,10 @@ __device__ inline double pose_from_x_warp(const double x[6], int map)
         const int m = lane % 3;
         const double xm = m == 0 ? x[0] : (m == 1 ? x[1] : x[2]);
         double sn, cs;
-        sincos(xm, &sn, &cs);
+        if (fabs(xm) <= kSmallAngle)
+            sincos_small(xm, sn, cs);
+        else
+            sincos(xm, &sn, &cs);
         const double sa = __shfl_sync(full, sn, 0), ca = __shfl_sync(full, cs, 0);
         const double sb = __shfl_sync(full, sn, 1), cb = __shfl_sync(full, cs, 1);
         const double sc = __shfl_sync(full, sn, 2), ccz = __shfl_sync(full, cs, 2);
@@ -316,23 +389,20 @@ __device__ inline double pose_from_x_warp(const double x[6], int map)
     else
     {
         const double w0 = x[0], w1 = x[1], w2 = x[2];
-        const double th2 = w0 * w0 + w1 * w1 + w2 * w2, th = sqrt(th2);
+        const double th2 = w0 * w0 + w1 * w1 + w2 * w2;
         double A, B, C;
-        if (th < 1e-4)
-        {
-            A = 1.0 - th2 / 6.0 + th2 * th2 / 120.0;
-            B = 0.5 - th2 / 24.0 + th2 * th2 / 720.0;
-            C = 1.0 / 6.0 - th2 / 120.0 + th2 * th2 / 5040.0;
-        }
+        if (th2 <= kSmallAngle * kSmallAngle)
+            exp_coeffs_small(th2, A, B, C); // no root, sine or division on the chain
         else
         {
+            const double th = sqrt(th2);
             double sn, cs;
             sincos(th, &sn, &cs);
             // the three coefficient divisions on three lanes
             const int m = lane % 3;
             const double num = m == 0 ? sn : (m == 1 ? 1.0 - cs : th - sn);
             const double den = m == 0 ? th : (m == 1 ? th2 : th2 * th);
-            const double q = num / den;
+            const double q = num * rcp_nr(den);
             A = __shfl_sync(full, q, 0);
             B = __shfl_sync(full, q, 1);
             C = __shfl_sync(full, q, 2);

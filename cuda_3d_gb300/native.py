@@ -149,6 +149,7 @@ _SIGS = {
     "gca3d_tracker_kernels": [_P, C.POINTER(_I64)],
     "gca3d_color_icp_vjp": [_P, _P, _P, C.POINTER(VjpParams), _P, _P, C.c_double, _P, C.POINTER(C.c_double), _P,
                             _P, _P, _P],
+    "gca3d_selfcheck_fp64": [_P, C.c_int, _P],
 }
 _RESTYPES = {"gca3d_status_string": C.c_char_p, "gca3d_last_error": C.c_char_p,
              "gca3d_kernel_launches": C.c_int64, "gca3d_stream": C.c_void_p}
@@ -409,6 +410,17 @@ def color_icp_batched(ctx, srcs, tgts, params, T_init=None):
     ctx.check(ctx.L.gca3d_color_icp_batched(ctx.h, P, cloud_array(srcs), cloud_array(tgts), C.byref(params),
                                             _ptr(Ti), res))
     return [result_dict(r) for r in res]
+
+
+def selfcheck_fp64(ctx, n=1 << 20):
+    """largest errors of the pose update's short FP64 routines on this device: Newton
+    reciprocal and small-angle sine / cosine in ulps against IEEE division and sincos,
+    and the exponential-map series' relative difference from the closed forms in units of
+    the closed forms' rounding bound"""
+    out = np.zeros(4, np.float64)
+    ctx.check(ctx.L.gca3d_selfcheck_fp64(ctx.h, int(n), out.ctypes.data_as(C.c_void_p)))
+    return {"rcp_ulp": float(out[0]), "sin_ulp": float(out[1]), "cos_ulp": float(out[2]),
+            "exp_coeff_vs_bound": float(out[3])}
 
 
 def color_icp_vjp(ctx, src, tgt, xi0, K=5, max_corr=0.05, lam=0.968, update_map=UPDATE_SE3_EXP, dT=None, dE=0.0,

@@ -419,6 +419,18 @@ int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt,
                         double dE, double T_out[16], double *E_out, double dxi0[6], float *d_dxyz,
                         float *d_drgb, int32_t *d_corr);
 
+/* ---------------------------------------------------------------------------
+ * self-check of the short FP64 routines of the pose update (no reference
+ * counterpart): over n sample points, out[0] = the largest error of the Newton
+ * reciprocal against IEEE 1/d in units in the last place (d over 2^-60 .. 2^60),
+ * out[1], out[2] = those of the small-angle sine and cosine against sincos
+ * (|x| <= 0.25), out[3] = the largest relative difference of the series for the
+ * exponential map's coefficients from their closed forms (rotation angle t in
+ * 0.05 .. 0.25), in units of the closed forms' own rounding bound eps (4 + 8 / t^2)
+ * (they cancel: 1 - cos t and t - sin t).
+ * ------------------------------------------------------------------------- */
+int gca3d_selfcheck_fp64(gca3d_context *ctx, int n, double out[4]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -238,3 +238,15 @@ def test_autotune_and_every_launch_shape_give_identical_results(ctx, N, synth):
         for a, b in zip(ref, got):
             np.testing.assert_array_equal(a["T"], b["T"])
             assert a["iterations"] == b["iterations"]
+
+
+def test_fp64_pose_routines_vs_cuda(ctx, N):
+    """The pose update's short FP64 routines on this device, against CUDA: the Newton
+    reciprocal within 1 ulp of IEEE division over 2^-60 .. 2^60, the small-angle
+    sine and cosine within 2 ulp of sincos for |x| <= 0.25, and the series of the
+    exponential map's coefficients within the rounding bound of the closed forms
+    (which cancel at small angles: eps (4 + 8 / t^2))."""
+    r = N.selfcheck_fp64(ctx, 1 << 20)
+    assert r["rcp_ulp"] <= 1.0
+    assert r["sin_ulp"] <= 2.0 and r["cos_ulp"] <= 2.0
+    assert r["exp_coeff_vs_bound"] <= 1.0
