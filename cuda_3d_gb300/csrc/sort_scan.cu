@@ -15,8 +15,8 @@ namespace gca3d
 {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems; // 2048 keys per tile
+constexpr int kSortItems = 12;
+constexpr int kSortTile = kSortThreads * kSortItems; // 3072 keys per tile
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kLookWindow = 8; // predecessor tiles read at once in the look-back
 
@@ -141,7 +141,7 @@ __global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *
     }
 }
 
-__global__ void __launch_bounds__(kSortThreads, 5) k_sort_pass(
+__global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, uint32_t *status,
     uint32_t *status_next, int64_t status_words, int pass, const int32_t *d_n, int *d_err)
 {
@@ -315,7 +315,8 @@ __global__ void __launch_bounds__(kSortThreads, 5) k_sort_pass(
 int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t cap, int max_bits,
                const int * /*d_key_bits*/)
 {
-    // five resident tiles per SM need the shared-memory side of the L1 carveout
+    // four resident tiles per SM (47 KB of shared memory each) need the shared-memory side
+    // of the L1 carveout
     static const bool carveout = cudaFuncSetAttribute(k_sort_pass, cudaFuncAttributePreferredSharedMemoryCarveout,
                                                       cudaSharedmemCarveoutMaxShared) == cudaSuccess;
     (void)carveout;
