@@ -60,27 +60,82 @@ template <bool Comp> struct Acc
         add(28, 1.0f);
         add(29, d2);
     }
-    // warp reduction; result valid in lane 0
-    __device__ __forceinline__ void warp_reduce()
+    // warp reduce-scatter by recursive halving: at the level of offset o a lane keeps
+    // half of its current terms (the upper half when its lane bit o is set) and adds
+    // the partner's copy of that half (xor o), sending the other half; 16 + 8 + 4 + 2 +
+    // 1 exchanges per value instead of 5 per term.  Lane t < kTerms ends with term t
+    // (value vs, error ve; terms 30 and 31 are zero padding).  The thread sums are
+    // plain, so the first level has no error terms to exchange.
+    __device__ __forceinline__ void warp_reduce_scatter(float &vs, float &ve) const
     {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-        {
-#pragma unroll
-            for (int k = 0; k < kTerms; ++k)
+        const unsigned full = 0xffffffffu;
+        const int lane = threadIdx.x & 31;
+        auto add2 = [](float a, float b, float ea, float eb, float &t, float &et) {
+            if (Comp)
             {
-                const float s2 = __shfl_down_sync(0xffffffffu, s[k], o);
-                if (Comp)
-                {
-                    const float e2 = __shfl_down_sync(0xffffffffu, e[k], o);
-                    const float t = s[k] + s2;
-                    const float bp = t - s[k];
-                    e[k] += e2 + ((s[k] - (t - bp)) + (s2 - bp));
-                    s[k] = t;
-                }
-                else
-                    s[k] += s2;
+                t = a + b;
+                const float bp = t - a;
+                et = ea + eb + ((a - (t - bp)) + (b - bp));
             }
+            else
+            {
+                t = a + b;
+                et = 0.0f;
+            }
+        };
+        float s16[16], e16[16];
+        {
+            const bool up = lane & 16;
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+            {
+                const float lo = s[k], hi = k + 16 < kTerms ? s[k + 16] : 0.0f;
+                const float keep = up ? hi : lo, send = up ? lo : hi;
+                add2(keep, __shfl_xor_sync(full, send, 16), 0.0f, 0.0f, s16[k], e16[k]);
+            }
+        }
+        float s8[8], e8[8];
+        {
+            const bool up = lane & 8;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+            {
+                const float keep = up ? s16[k + 8] : s16[k], send = up ? s16[k] : s16[k + 8];
+                const float ekeep = up ? e16[k + 8] : e16[k], esend = up ? e16[k] : e16[k + 8];
+                add2(keep, __shfl_xor_sync(full, send, 8), ekeep, Comp ? __shfl_xor_sync(full, esend, 8) : 0.0f,
+                     s8[k], e8[k]);
+            }
+        }
+        float s4[4], e4[4];
+        {
+            const bool up = lane & 4;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                const float keep = up ? s8[k + 4] : s8[k], send = up ? s8[k] : s8[k + 4];
+                const float ekeep = up ? e8[k + 4] : e8[k], esend = up ? e8[k] : e8[k + 4];
+                add2(keep, __shfl_xor_sync(full, send, 4), ekeep, Comp ? __shfl_xor_sync(full, esend, 4) : 0.0f,
+                     s4[k], e4[k]);
+            }
+        }
+        float s2[2], e2[2];
+        {
+            const bool up = lane & 2;
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+            {
+                const float keep = up ? s4[k + 2] : s4[k], send = up ? s4[k] : s4[k + 2];
+                const float ekeep = up ? e4[k + 2] : e4[k], esend = up ? e4[k] : e4[k + 2];
+                add2(keep, __shfl_xor_sync(full, send, 2), ekeep, Comp ? __shfl_xor_sync(full, esend, 2) : 0.0f,
+                     s2[k], e2[k]);
+            }
+        }
+        {
+            const bool up = lane & 1;
+            const float keep = up ? s2[1] : s2[0], send = up ? s2[0] : s2[1];
+            const float ekeep = up ? e2[1] : e2[0], esend = up ? e2[0] : e2[1];
+            add2(keep, __shfl_xor_sync(full, send, 1), ekeep, Comp ? __shfl_xor_sync(full, esend, 1) : 0.0f, vs,
+                 ve);
         }
     }
     __device__ __forceinline__ double value(int k) const
@@ -99,14 +154,13 @@ __device__ __forceinline__ void block_reduce_store(Acc<Comp> &acc, double *part)
     __shared__ float s_s[kIcpThreads / 32][kTerms];
     __shared__ float s_e[kIcpThreads / 32][kTerms];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    acc.warp_reduce();
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < kTerms; ++k)
-        {
-            s_s[warp][k] = acc.s[k];
-            s_e[warp][k] = acc.e[k];
-        }
+    float vs, ve;
+    acc.warp_reduce_scatter(vs, ve); // lane k holds term k
+    if (lane < kTerms)
+    {
+        s_s[warp][lane] = vs;
+        s_e[warp][lane] = ve;
+    }
     __syncthreads();
     if (threadIdx.x < kTerms)
     {
