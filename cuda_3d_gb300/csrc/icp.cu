@@ -430,9 +430,10 @@ __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restr
     }
 }
 
-// step 2: residuals, Jacobians, block sums (one partial per block)
+// step 2: residuals, Jacobians, block sums (one partial per block); three resident
+// blocks per SM (80 registers: the 30 sums and two points' gathers in flight)
 template <bool Comp>
-__global__ void __launch_bounds__(kIcpThreads) k_icp_accum(const float4 *__restrict__ src_pos, const int32_t *src_off,
+__global__ void __launch_bounds__(kIcpThreads, 3) k_icp_accum(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                            const float4 *__restrict__ tpos,
                                                            const float4 *__restrict__ attr0,
                                                            const float4 *__restrict__ attr1,
