@@ -479,10 +479,41 @@ int gca3d_cloud_destroy(gca3d_cloud *c)
     return GCA3D_OK;
 }
 
+// the device address of a buffer the device can read in place: pinned (page-locked)
+// host memory, device or managed memory; null for pageable host memory (which is
+// copied through a staging buffer instead)
+static const float *device_readable(const float *p)
+{
+    if (!p)
+        return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return static_cast<const float *>(a.devicePointer);
+    return nullptr;
+}
+
 int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *c, const float *xyz, const float *rgb, int64_t n)
 {
     if (!ctx || !c || (!xyz && n > 0) || n < 0 || n > c->capacity)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "cloud_upload: bad arguments or n > capacity");
+    if (n > 0)
+    {
+        // pinned host buffers (and device ones) are read by the packing kernel in place:
+        // one transfer, no staging copy
+        const float *dx = device_readable(xyz), *dc = rgb ? device_readable(rgb) : nullptr;
+        if (dx && (!rgb || dc))
+        {
+            k_pack<<<grid_for(n), kBlock, 0, ctx->stream>>>(dx, dc, (int)n, c->pos, c->col, c->d_count);
+            GCA_CHECK_LAUNCH(ctx);
+            c->has_normals = c->has_grad = false;
+            return GCA3D_OK;
+        }
+    }
     ctx->arena.reset();
     float *sx = ctx->arena.get<float>(3 * std::max<int64_t>(n, 1));
     float *sc = rgb ? ctx->arena.get<float>(3 * std::max<int64_t>(n, 1)) : nullptr;

@@ -146,7 +146,10 @@ int gca3d_copy(gca3d_context *ctx, void *dst, const void *src, int64_t bytes);
 /* reference: gca::point_cloud(size_t) (src/geometry/point_cloud.hpp:26) */
 int gca3d_cloud_create(gca3d_context *ctx, int64_t capacity, gca3d_cloud **cloud);
 int gca3d_cloud_destroy(gca3d_cloud *cloud);
-/* xyz, rgb: n x 3 floats, host or device memory.  rgb may be NULL (black).
+/* xyz, rgb: n x 3 floats, host or device memory.  rgb may be NULL (black).  Pinned
+ * host memory (and device memory) is read in place by the packing kernel on the
+ * context stream, so, as with cudaMemcpyAsync, it must not change before the stream
+ * has passed the call; pageable host memory goes through a staging copy.
  * reference: point_cloud::create_from_pcl (src/geometry/point_cloud.cu:481-504) */
 int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *cloud, const float *xyz,
                        const float *rgb, int64_t n);

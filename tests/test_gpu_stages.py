@@ -51,6 +51,35 @@ def test_upload_download_roundtrip(ctx, golden, orc):
     np.testing.assert_array_equal(d["rgb"], rgb)
 
 
+def test_upload_from_pinned_and_device_memory(ctx, N, golden):
+    """Pinned host buffers and device buffers are read in place by the packing
+    kernel; pageable ones go through a staging copy.  All three give the same cloud
+    (positions with the intensity the ICP uses, and colours)."""
+    torch = pytest.importorskip("torch")
+    xyz, rgb = golden["cloud_xyz"], golden["cloud_rgb"]
+    n = len(xyz)
+
+    def device_arrays(c):
+        pos, col = np.empty((n, 4), np.float32), np.empty((n, 4), np.float32)
+        views = c.device_views()
+        ctx.check(ctx.L.gca3d_copy(ctx.h, pos.ctypes.data_as(C.c_void_p), C.c_void_p(views[0]), n * 16))
+        ctx.check(ctx.L.gca3d_copy(ctx.h, col.ctypes.data_as(C.c_void_p), C.c_void_p(views[1]), n * 16))
+        return pos, col
+
+    want = device_arrays(ctx.cloud_from(xyz, rgb))
+    pinned = [torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory() for a in (xyz, rgb)]
+    device = [t.to("cuda") for t in pinned]
+    torch.cuda.synchronize()
+    for bufs in (pinned, device):
+        c = N.Cloud(ctx, n)
+        ctx.check(ctx.L.gca3d_cloud_upload(ctx.h, c.h, C.c_void_p(bufs[0].data_ptr()), C.c_void_p(bufs[1].data_ptr()),
+                                           n))
+        got = device_arrays(c)
+        assert len(c) == n
+        np.testing.assert_array_equal(got[0], want[0])
+        np.testing.assert_array_equal(got[1], want[1])
+
+
 def test_bounds_true_max(ctx, golden):
     for pts in (golden["cloud_xyz"], golden.voxel_input("neg05")[0]):
         c = ctx.cloud_from(pts)
