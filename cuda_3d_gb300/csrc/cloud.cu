@@ -134,6 +134,46 @@ __global__ void k_pack(const float *__restrict__ xyz, const float *__restrict__ 
     col[i] = make_float4(r, g, b, 0.0f);
 }
 
+// many clouds' uploads in one launch: descriptors by value (kUploadChunk per launch,
+// under the 4 KB parameter limit); a block packs part of one cloud
+constexpr int kUploadChunk = 64;
+struct UploadDesc
+{
+    const float *xyz, *rgb;
+    float4 *pos, *col;
+    int32_t *d_count;
+    int n, first; // points, first block
+};
+struct UploadBatch
+{
+    int count;
+    UploadDesc d[kUploadChunk];
+};
+
+__global__ void k_pack_many(const __grid_constant__ UploadBatch B)
+{
+    // the block's cloud: the last one whose first block is <= blockIdx.x
+    int lo = 0, hi = B.count - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (B.d[mid].first <= (int)blockIdx.x)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const UploadDesc &D = B.d[lo];
+    const int i = ((int)blockIdx.x - D.first) * (int)blockDim.x + (int)threadIdx.x;
+    if (i == 0)
+        *D.d_count = D.n;
+    if (i >= D.n)
+        return;
+    const float *rgb = D.rgb, *xyz = D.xyz;
+    const float r = rgb ? rgb[3 * i] : 0.0f, g = rgb ? rgb[3 * i + 1] : 0.0f, b = rgb ? rgb[3 * i + 2] : 0.0f;
+    D.pos[i] = make_float4(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], intensity_of(r, g, b));
+    D.col[i] = make_float4(r, g, b, 0.0f);
+}
+
 __global__ void k_pack3(const float *__restrict__ v, int n, float4 *out)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -529,6 +569,51 @@ int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *c, const float *xyz, con
     GCA_CHECK_LAUNCH(ctx);
     c->has_normals = c->has_grad = false;
     return GCA3D_OK;
+}
+
+int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *clouds, const float *const *xyz,
+                            const float *const *rgb, const int64_t *n)
+{
+    if (!ctx || count < 0 || (count > 0 && (!clouds || !xyz || !n)))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "cloud_upload_many: bad arguments");
+    for (int k = 0; k < count; ++k)
+        if (!clouds[k] || (!xyz[k] && n[k] > 0) || n[k] < 0 || n[k] > clouds[k]->capacity)
+            return fail(ctx, GCA3D_ERR_INVALID_VALUE, "cloud_upload_many: bad arguments or n > capacity");
+    UploadBatch B;
+    B.count = 0;
+    int blocks = 0;
+    auto flush = [&]() -> int {
+        if (B.count == 0)
+            return GCA3D_OK;
+        k_pack_many<<<blocks, kBlock, 0, ctx->stream>>>(B);
+        GCA_CHECK_LAUNCH(ctx);
+        B.count = 0;
+        blocks = 0;
+        return GCA3D_OK;
+    };
+    for (int k = 0; k < count; ++k)
+    {
+        gca3d_cloud *c = clouds[k];
+        const float *ck = rgb ? rgb[k] : nullptr;
+        const float *dx = n[k] > 0 ? device_readable(xyz[k]) : nullptr, *dc = ck ? device_readable(ck) : nullptr;
+        int st = GCA3D_OK;
+        if (n[k] > 0 && (!dx || (ck && !dc)))
+            st = gca3d_cloud_upload(ctx, c, xyz[k], ck, n[k]); // pageable: staged on its own
+        else
+        {
+            if (B.count == kUploadChunk)
+                st = flush();
+            if (!st)
+            {
+                B.d[B.count++] = UploadDesc{dx, dc, c->pos, c->col, c->d_count, (int)n[k], blocks};
+                blocks += std::max(grid_for(n[k]), 1);
+                c->has_normals = c->has_grad = false;
+            }
+        }
+        if (st)
+            return st;
+    }
+    return flush();
 }
 
 int gca3d_cloud_set_normals(gca3d_context *ctx, gca3d_cloud *c, const float *nrm, int64_t n)

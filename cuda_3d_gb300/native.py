@@ -103,6 +103,7 @@ _SIGS = {
     "gca3d_cloud_create": [_P, _I64, C.POINTER(_P)],
     "gca3d_cloud_destroy": [_P],
     "gca3d_cloud_upload": [_P, _P, _P, _P, _I64],
+    "gca3d_cloud_upload_many": [_P, C.c_int, _P, _P, _P, _P],
     "gca3d_cloud_set_normals": [_P, _P, _P, _I64],
     "gca3d_cloud_set_gradients": [_P, _P, _P, _I64],
     "gca3d_cloud_capacity": [_P, C.POINTER(_I64)],
@@ -361,6 +362,16 @@ def result_dict(r):
 def cloud_array(clouds):
     arr = (C.c_void_p * len(clouds))(*[c.h.value for c in clouds])
     return arr
+
+
+def upload_many(ctx, clouds, xyz_ptrs, rgb_ptrs, counts):
+    """gca3d_cloud_upload_many: raw buffer addresses (pinned host or device memory is
+    read in place), one call for all clouds"""
+    k = len(clouds)
+    xa = (C.c_void_p * k)(*[int(p) for p in xyz_ptrs])
+    ra = (C.c_void_p * k)(*[int(p) if p else None for p in rgb_ptrs])
+    na = (C.c_int64 * k)(*[int(v) for v in counts])
+    ctx.check(ctx.L.gca3d_cloud_upload_many(ctx.h, k, cloud_array(clouds), xa, ra, na))
 
 
 class IcpPlan:

@@ -153,6 +153,13 @@ int gca3d_cloud_destroy(gca3d_cloud *cloud);
  * reference: point_cloud::create_from_pcl (src/geometry/point_cloud.cu:481-504) */
 int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *cloud, const float *xyz,
                        const float *rgb, int64_t n);
+/* count uploads in one call (no reference counterpart: the reference creates clouds
+ * one at a time): cloud k gets xyz[k], rgb[k] (rgb or rgb[k] may be NULL), n[k]
+ * points, as gca3d_cloud_upload.  The clouds whose buffers the device can read in
+ * place (pinned host or device memory) are packed by one kernel launch per 64;
+ * the others go through gca3d_cloud_upload's staging copy. */
+int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *clouds,
+                            const float *const *xyz, const float *const *rgb, const int64_t *n);
 /* normals (n x 3) supplied by the caller; marks the cloud as having normals */
 int gca3d_cloud_set_normals(gca3d_context *ctx, gca3d_cloud *cloud, const float *nrm, int64_t n);
 /* colour gradients (n x 3) supplied by the caller; needs normals */

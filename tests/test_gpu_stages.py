@@ -80,6 +80,37 @@ def test_upload_from_pinned_and_device_memory(ctx, N, golden):
         np.testing.assert_array_equal(got[1], want[1])
 
 
+def test_upload_many_matches_single_uploads(ctx, N, golden):
+    """One batched call over clouds of mixed sources (pinned, device, pageable, no
+    colour, empty) gives the clouds of the single uploads."""
+    torch = pytest.importorskip("torch")
+    xyz, rgb = golden["cloud_xyz"], golden["cloud_rgb"]
+    n = len(xyz)
+    parts = [(0, n), (0, 1000), (5, 4000), (100, 100), (7, n)]
+    pinned = [torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory() for a in (xyz, rgb)]
+    device = [t.to("cuda") for t in pinned]
+    torch.cuda.synchronize()
+    pageable = [np.ascontiguousarray(a, np.float32) for a in (xyz, rgb)]
+    srcs = [pinned, device, pageable, pinned, device]
+    clouds, xp, rp, cnt, want = [], [], [], [], []
+    for k, ((a, b), bufs) in enumerate(zip(parts, srcs)):
+        ptr = (lambda t, off: t.data_ptr() + 12 * off) if bufs is not pageable else \
+              (lambda t, off: t.ctypes.data + 12 * off)
+        with_rgb = k != 1
+        clouds.append(N.Cloud(ctx, max(b - a, 1)))
+        xp.append(ptr(bufs[0], a))
+        rp.append(ptr(bufs[1], a) if with_rgb else None)
+        cnt.append(b - a)
+        ref = ctx.cloud_from(xyz[a:b], rgb[a:b] if with_rgb else None, capacity=max(b - a, 1))
+        want.append(ref.download())
+    N.upload_many(ctx, clouds, xp, rp, cnt)
+    for c, w, m in zip(clouds, want, cnt):
+        assert len(c) == m
+        d = c.download()
+        np.testing.assert_array_equal(d["xyz"], w["xyz"])
+        np.testing.assert_array_equal(d["rgb"], w["rgb"])
+
+
 def test_bounds_true_max(ctx, golden):
     for pts in (golden["cloud_xyz"], golden.voxel_input("neg05")[0]):
         c = ctx.cloud_from(pts)
