@@ -519,10 +519,11 @@ int gca3d_cloud_destroy(gca3d_cloud *c)
     return GCA3D_OK;
 }
 
-// the device address of a buffer the device can read in place: pinned (page-locked)
-// host memory, device or managed memory; null for pageable host memory (which is
-// copied through a staging buffer instead)
-static const float *device_readable(const float *p)
+// the device address of a buffer the context's device can read in place: pinned
+// (page-locked, mapped) host memory or memory of that device; null for anything
+// else -- pageable or managed host memory, another device's memory -- which is
+// copied through a staging buffer instead
+static const float *device_readable(const gca3d_context *ctx, const float *p)
 {
     if (!p)
         return nullptr;
@@ -532,7 +533,7 @@ static const float *device_readable(const float *p)
         cudaGetLastError();
         return nullptr;
     }
-    if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+    if (a.type == cudaMemoryTypeHost || (a.type == cudaMemoryTypeDevice && a.device == ctx->device))
         return static_cast<const float *>(a.devicePointer);
     return nullptr;
 }
@@ -545,7 +546,7 @@ int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *c, const float *xyz, con
     {
         // pinned host buffers (and device ones) are read by the packing kernel in place:
         // one transfer, no staging copy
-        const float *dx = device_readable(xyz), *dc = rgb ? device_readable(rgb) : nullptr;
+        const float *dx = device_readable(ctx, xyz), *dc = rgb ? device_readable(ctx, rgb) : nullptr;
         if (dx && (!rgb || dc))
         {
             k_pack<<<grid_for(n), kBlock, 0, ctx->stream>>>(dx, dc, (int)n, c->pos, c->col, c->d_count);
@@ -595,7 +596,8 @@ int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *c
     {
         gca3d_cloud *c = clouds[k];
         const float *ck = rgb ? rgb[k] : nullptr;
-        const float *dx = n[k] > 0 ? device_readable(xyz[k]) : nullptr, *dc = ck ? device_readable(ck) : nullptr;
+        const float *dx = n[k] > 0 ? device_readable(ctx, xyz[k]) : nullptr;
+        const float *dc = ck ? device_readable(ctx, ck) : nullptr;
         int st = GCA3D_OK;
         if (n[k] > 0 && (!dx || (ck && !dc)))
             st = gca3d_cloud_upload(ctx, c, xyz[k], ck, n[k]); // pageable: staged on its own

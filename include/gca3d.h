@@ -147,17 +147,18 @@ int gca3d_copy(gca3d_context *ctx, void *dst, const void *src, int64_t bytes);
 int gca3d_cloud_create(gca3d_context *ctx, int64_t capacity, gca3d_cloud **cloud);
 int gca3d_cloud_destroy(gca3d_cloud *cloud);
 /* xyz, rgb: n x 3 floats, host or device memory.  rgb may be NULL (black).  Pinned
- * host memory (and device memory) is read in place by the packing kernel on the
- * context stream, so, as with cudaMemcpyAsync, it must not change before the stream
- * has passed the call; pageable host memory goes through a staging copy.
+ * host memory (and memory of the context's device) is read in place by the packing
+ * kernel on the context stream, so, as with cudaMemcpyAsync, it must not change
+ * before the stream has passed the call; pageable or managed host memory and other
+ * devices' memory go through a staging copy.
  * reference: point_cloud::create_from_pcl (src/geometry/point_cloud.cu:481-504) */
 int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *cloud, const float *xyz,
                        const float *rgb, int64_t n);
 /* count uploads in one call (no reference counterpart: the reference creates clouds
  * one at a time): cloud k gets xyz[k], rgb[k] (rgb or rgb[k] may be NULL), n[k]
- * points, as gca3d_cloud_upload.  The clouds whose buffers the device can read in
- * place (pinned host or device memory) are packed by one kernel launch per 64;
- * the others go through gca3d_cloud_upload's staging copy. */
+ * points, as gca3d_cloud_upload.  The clouds whose buffers the device reads in place
+ * (pinned host memory, memory of the context's device) are packed by one kernel
+ * launch per 64; the others go through gca3d_cloud_upload's staging copy. */
 int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *clouds,
                             const float *const *xyz, const float *const *rgb, const int64_t *n);
 /* normals (n x 3) supplied by the caller; marks the cloud as having normals */
