@@ -272,6 +272,9 @@ __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double
 #pragma unroll
     for (int k = 0; k < 6; ++k)
     {
+        // every diagonal lane's reciprocal, computed while the pivot is searched (the
+        // chosen one is broadcast below, so the division is off the pivot's chain)
+        const double ra = diag ? rcp_nr(a) : 0.0;
         // symmetric pivot: the largest remaining diagonal entry (first one on ties);
         // magnitudes compared as the bit patterns of |A[i][i]|
         const long long mag = diag ? (__double_as_longlong(a) & 0x7fffffffffffffffll) : -1ll;
@@ -296,6 +299,7 @@ __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double
             perm = (perm & ~((15u << (4 * k)) | (15u << (4 * piv)))) | (pp << (4 * k)) | (pk << (4 * piv));
         }
         const double Dk = __shfl_sync(full, a, tri_lane(k, k));
+        const double rk = __shfl_sync(full, ra, tri_lane(piv, piv)); // 1 / Dk (before the swap)
         const bool lcol = mat && lj == k && li > k;
         if (fabs(Dk) <= kTiny)
         {
@@ -305,7 +309,7 @@ __device__ inline int solve6_warp(const double *S /* 21 upper + 6 rhs */, double
         }
         else
         {
-            const double inv = rcp_nr(Dk); // one reciprocal per pivot
+            const double inv = rk; // one reciprocal per pivot
             if (lcol)
                 a *= inv;
             const bool upd = mat && lj > k;
