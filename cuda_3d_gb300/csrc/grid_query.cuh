@@ -134,22 +134,6 @@ struct NNBest
     int t;
 };
 
-// nearest grid point with d^2 < rr; ties on d^2 go to the smaller original index
-__device__ __forceinline__ NNBest nn_search_one(const GridDev &g, const KeyLayout &L, int seg, float3 o, float3 p,
-                                                float rr)
-{
-    NNBest b{rr, -1};
-    grid_visit(g, L, seg, o, p, [&](int t, float4 q) {
-        const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
-        if (d2 < b.d2 || (d2 == b.d2 && b.t >= 0 && __ldg(&g.sidx[t]) < __ldg(&g.sidx[b.t])))
-        {
-            b.d2 = d2;
-            b.t = t;
-        }
-    });
-    return b;
-}
-
 // ---------------------------------------------------------------------------
 // 4 lanes per query: lane `sub` of a 4-lane group probes and scans rows
 // sub, sub + 4, sub + 8 of the 9, so the dependent chain of a query is a third
