@@ -133,16 +133,25 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
-        self.index = index
+    def __init__(self, local=0):
+        self.gpu_id = self.smi_id(local)
         self.proc = None
         self.path = None
+
+    @staticmethod
+    def smi_id(local):
+        """the device's UUID as nvidia-smi names it: under CUDA_VISIBLE_DEVICES the CUDA
+        ordinal is not the nvidia-smi index, the UUID is the same in both"""
+        import torch
+
+        u = str(torch.cuda.get_device_properties(local).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
 
     def start(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu_id}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
@@ -162,7 +171,10 @@ class ClockSampler:
             if len(parts) >= 9:
                 rows.append(parts)
         os.unlink(self.path)
-        return self.summarise(rows)
+        out = self.summarise(rows)
+        if out is not None:
+            out["gpu_id"] = self.gpu_id
+        return out
 
     @staticmethod
     def summarise(rows):
@@ -219,6 +231,34 @@ def icp_algorithmic_bytes(results):
     return total
 
 
+def workload_config(pairs, world):
+    """the workload description both arms print (the reference arm times a sample of it)"""
+    n_src = sum(len(p.src_xyz) for p in pairs)
+    n_tgt = sum(len(p.tgt_xyz) for p in pairs)
+    return {"workload": "batch64: 64 fragment pairs, clouds log-uniform 20k-300k points, rot 0-15 deg, "
+                        "trans 0-15 cm, overlap 40-90 %, scales voxel 0.04/0.02/0.01 m x 50/30/14 iterations",
+            "pairs_per_gpu": len(pairs), "src_points": n_src, "tgt_points": n_tgt,
+            "scales": SCALES, "parallelism": f"replicas x{world} (pairs sharded per rank)",
+            "l2": f"inputs larger than L2 ({(n_src + n_tgt) * 32 / 1e6:.0f} MB resident SoA)"}
+
+
+def cpu_sample(pairs, k=4):
+    """the fixed pair sample the CPU measurements time: pairs ranked by point count
+    (source + target), one at the middle of each of k equal rank strata, so the sample
+    spans the batch's size range"""
+    k = min(k, len(pairs))
+    order = sorted(range(len(pairs)), key=lambda i: len(pairs[i].src_xyz) + len(pairs[i].tgt_xyz))
+    return sorted(order[(2 * j + 1) * len(pairs) // (2 * k)] for j in range(k))
+
+
+def sample_text(pairs, idx):
+    pts = sum(len(pairs[i].src_xyz) + len(pairs[i].tgt_xyz) for i in idx) / len(idx)
+    mean = sum(len(p.src_xyz) + len(p.tgt_xyz) for p in pairs) / len(pairs)
+    return (f"pairs {idx} of the batch (one per size stratum; {pts / 1e3:.0f}k points per pair against the "
+            f"batch's mean {mean / 1e3:.0f}k), full three-scale schedule, FP32 in the reference's operation order "
+            f"(oracle/gca_oracle.c), OpenMP")
+
+
 def pose_spread(a, b):
     from cuda_3d_gb300 import synth
 
@@ -245,8 +285,6 @@ def run_ours(args):
     ctx = N.Context(local, stream=stream.cuda_stream)
     pairs = make_workload(args.pairs, rank_seed(args.seed, rank))
     P = len(pairs)
-    n_src = sum(len(p.src_xyz) for p in pairs)
-    n_tgt = sum(len(p.tgt_xyz) for p in pairs)
     srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
     tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
     scales = [N.scale(*s) for s in SCALES]
@@ -352,45 +390,58 @@ def run_ours(args):
                 "avg_launch_us": icp_ms * 1e3 / max(icp_launches, 1), "launches": icp_launches}
 
     # ---- plain: one pair per call, FP32, host convergence checks ----------------
-    plain = None
+    # the 64 single-pair plans are built before the timed region (the timed calls
+    # launch and read back only); the one-shot call that builds and frees its plan
+    # every time is reported beside it
+    plain, res_plain = None, None
     if not args.no_plain:
         pp = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, compensated=False, use_graph=False)
-        res_plain = [N.color_icp(ctx, s, t, pp) for s, t in zip(srcs, tgts)]
+        plans = [N.IcpPlan(ctx, [s], [t], pp) for s, t in zip(srcs, tgts)]
+        res_plain = [pl.execute(results=True)[0] for pl in plans]
+        reps = 2
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        reps = 2
         for _ in range(reps):
-            res_plain = [N.color_icp(ctx, s, t, pp) for s, t in zip(srcs, tgts)]
+            res_plain = [pl.execute(results=True)[0] for pl in plans]
         torch.cuda.synchronize()
         ms_plain = reduce_max((time.perf_counter() - t0) * 1e3 / reps, "cuda")
+        del plans
+        [N.color_icp(ctx, s, t, pp) for s, t in zip(srcs, tgts)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res_once = [N.color_icp(ctx, s, t, pp) for s, t in zip(srcs, tgts)]
+        torch.cuda.synchronize()
+        ms_once = reduce_max((time.perf_counter() - t0) * 1e3, "cuda")
         rot, tr = pose_spread(res_chosen, res_plain)
+        assert all(np.array_equal(a["T"], b["T"]) for a, b in zip(res_plain, res_once))
         plain = {"value": world * P / (ms_plain / 1000.0), "unit": "pairs/s", "ms_per_step": ms_plain,
-                 "chosen_over_plain": (world * P / (ms / 1000.0)) / (world * P / (ms_plain / 1000.0)),
-                 "max_pose_diff_vs_chosen": {"rad": rot, "m": tr}}
+                 "chosen_over_plain": ms_plain / ms,
+                 "max_pose_diff_vs_chosen": {"rad": rot, "m": tr},
+                 "with_plan_setup": {"value": world * P / (ms_once / 1000.0), "unit": "pairs/s",
+                                     "ms_per_step": ms_once, "chosen_over_plain": ms_once / ms,
+                                     "note": "gca3d_color_icp per pair: plan built (device allocations, "
+                                             "host-pinned buffers) and freed in every call"}}
 
     gt = [synth.pose_error(r["T"], p.T_gt) for r, p in zip(res_chosen, pairs)]
     rows = None
     if rank == 0 and not args.no_extras:
         rows = run_rows(ctx, N, synth, args)
-    cpu = None
+    cpu, pose_check = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(pairs, sample=4)
+        cpu, pose_check = cpu_leg(pairs, res_chosen, res_plain)
 
     line = {
         "metric": "colored-ICP pairs/s (64-pair batch, three-scale)",
         "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (FP64 solve and cross-block sums)", "data": "synthetic",
-        "config": {"workload": "batch64: 64 fragment pairs, clouds log-uniform 20k-300k points, rot 0-15 deg, "
-                               "trans 0-15 cm, overlap 40-90 %, scales voxel 0.04/0.02/0.01 m x 50/30/14 iterations",
-                   "pairs_per_gpu": P, "src_points": n_src, "tgt_points": n_tgt,
-                   "scales": SCALES, "parallelism": f"replicas x{world} (pairs sharded per rank)",
-                   "tuning": tuning,
-                   "l2": f"inputs larger than L2 ({(n_src + n_tgt) * 32 / 1e6:.0f} MB resident SoA)"},
+        "config": workload_config(pairs, world),
+        "tuning": tuning,
         "e2e": e2e,
         "roofline": roofline,
         "cpu_baseline": cpu,
         "plain": plain,
+        "pose_vs_fp64_oracle": pose_check,
         "kernel_breakdown_ms_per_execute": breakdown,
         "rows": rows,
         "gt_error_max": {"rad": max(g[0] for g in gt), "m": max(g[1] for g in gt)},
@@ -512,21 +563,45 @@ def run_rows(ctx, N, synth, args):
 # --------------------------------------------------------------------------- #
 # CPU: the reference's algorithm on the host cores
 # --------------------------------------------------------------------------- #
-def cpu_baseline(pairs, sample=4):
+def cpu_leg(pairs, res_chosen, res_plain):
+    """the CPU baseline (the reference's FP32 algorithm timed on the sample pairs) and,
+    untimed, the FP64 oracle as the checker of both GPU arms' poses on every pair"""
+    from cuda_3d_gb300 import synth
+
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     scales = [O.Scale(*s) for s in SCALES]
-    sub = pairs[:sample]
+    idx = cpu_sample(pairs)
     t0 = time.perf_counter()
-    for p in sub:
+    for i in idx:
+        p = pairs[i]
         O.multiscale_ref32(p.src_xyz, p.src_rgb, p.tgt_xyz, p.tgt_rgb, scales)
     dt = time.perf_counter() - t0
-    return {"value": len(sub) / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
-            "sample": f"pairs 0-{len(sub) - 1} of the batch, full three-scale schedule, "
-                      f"FP32 in the reference's operation order (oracle/gca_oracle.c), OpenMP"}
+    cpu = {"value": len(idx) / dt, "unit": "pairs/s", "cores": threads, "kind": "port",
+           "sample": sample_text(pairs, idx)}
+
+    runs = [O.multiscale_f64(p.src_xyz, p.src_rgb, p.tgt_xyz, p.tgt_rgb, scales, update_map=O.UPDATE_SE3_EXP)
+            for p in pairs]
+    check = {"pairs": len(pairs), "tolerance": {"rad": 1e-5, "m": 1e-5},
+             "definition": "rotation angle of R_gpu R_fp64^T and |t_gpu - t_fp64| per pair, FP64 oracle "
+                           "(oracle/gca_oracle.c) on the same clouds and schedule"}
+    gt = [synth.pose_error(T, p.T_gt) for (T, _), p in zip(runs, pairs)]
+    check["oracle_gt_error_max"] = {"rad": max(g[0] for g in gt), "m": max(g[1] for g in gt),
+                                    "pair": int(np.argmax([g[0] for g in gt]))}
+    for name, res in (("chosen", res_chosen), ("plain", res_plain)):
+        if res is None:
+            continue
+        e = np.array([synth.pose_error(r["T"], T) for r, (T, _) in zip(res, runs)])
+        same_it = all(list(r["scale_iterations"][:len(SCALES)]) == [x.iterations for x in rr]
+                      for r, (_, rr) in zip(res, runs))
+        check[name] = {"max": {"rad": float(e[:, 0].max()), "m": float(e[:, 1].max())},
+                       "median": {"rad": float(np.median(e[:, 0])), "m": float(np.median(e[:, 1]))},
+                       "worst_pair": int(np.argmax(e.max(1))), "iterations_equal_oracle": same_it,
+                       "within_tolerance": bool((e <= 1e-5).all())}
+    return cpu, check
 
 
 def run_reference(args):
@@ -541,14 +616,11 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     scales = [O.Scale(*s) for s in SCALES]
-    per_step = 2
-    k = 0
+    idx = cpu_sample(pairs)
 
     def step():
-        nonlocal k
-        for _ in range(per_step):
-            p = pairs[k % len(pairs)]
-            k += 1
+        for i in idx:
+            p = pairs[i]
             O.multiscale_ref32(p.src_xyz, p.src_rgb, p.tgt_xyz, p.tgt_rgb, scales)
 
     for _ in range(args.warmup):
@@ -557,15 +629,14 @@ def run_reference(args):
     for _ in range(args.steps):
         step()
     dt = (time.perf_counter() - t0) / args.steps
-    value = per_step / dt
-    sample = (f"{per_step} pairs per step (cycling through the 64-pair batch), full three-scale schedule, "
-              f"FP32 in the reference's operation order (oracle/gca_oracle.c), OpenMP")
+    value = len(idx) / dt
     print(json.dumps({
         "impl": "reference", "metric": "colored-ICP pairs/s (64-pair batch, three-scale)", "value": value,
         "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batch64 (as the ours arm)", "pairs_per_step": per_step},
-        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port", "sample": sample},
+        "config": workload_config(pairs, world),
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": "each step: " + sample_text(pairs, idx)},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 

@@ -599,11 +599,21 @@ int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *c
         const float *dx = n[k] > 0 ? device_readable(ctx, xyz[k]) : nullptr;
         const float *dc = ck ? device_readable(ctx, ck) : nullptr;
         int st = GCA3D_OK;
+        // the writes land in call order: queued in-place entries are packed before a
+        // staged upload, and before a second entry for a cloud already queued (two
+        // entries of one launch would race on the same cloud)
+        bool queued = false;
+        for (int j = 0; j < B.count; ++j)
+            queued = queued || B.d[j].pos == c->pos;
         if (n[k] > 0 && (!dx || (ck && !dc)))
-            st = gca3d_cloud_upload(ctx, c, xyz[k], ck, n[k]); // pageable: staged on its own
+        {
+            st = flush();
+            if (!st)
+                st = gca3d_cloud_upload(ctx, c, xyz[k], ck, n[k]); // pageable: staged on its own
+        }
         else
         {
-            if (B.count == kUploadChunk)
+            if (B.count == kUploadChunk || queued)
                 st = flush();
             if (!st)
             {

@@ -149,10 +149,23 @@ __device__ bool smallest_eigvec_f32(float a00, float a01, float a02, float a11, 
     r = fminf(fmaxf(r, -1.0f), 1.0f);
     const float phi = acosf(r) * (1.0f / 3.0f);
     const float lmax = q + 2.0f * p * cosf(phi);
-    const float lmin = q + 2.0f * p * cosf(phi + 2.0943951023931957f);
+    float lmin = q + 2.0f * p * cosf(phi + 2.0943951023931957f);
     const float lmid = 3.0f * q - lmax - lmin;
     if (!(lmid - lmin > 1e-3f * (lmax - lmin)))
         return false;
+    // One Newton step on det(A - l I) = 0 from the trigonometric lmin.  Where two
+    // eigenvalues are close, r is near +-1 and acos(r) is ill-conditioned, so lmin
+    // carries an error of order sqrt(eps) p; the cross products below turn an error d in
+    // lmin into an angle of about d / (lmid - lmin).  With B = A - lmin I the step is
+    // lmin += det(B) / (sum of the principal 2x2 minors of B), the minors' sum being
+    // -d/dl det(A - l I); it is about (lmid - lmin)(lmax - lmin) > 0 here.
+    {
+        const float c0 = a00 - lmin, c1 = a11 - lmin, c2 = a22 - lmin;
+        const float m2 = (c0 * c1 - a01 * a01) + (c0 * c2 - a02 * a02) + (c1 * c2 - a12 * a12);
+        const float dB = c0 * (c1 * c2 - a12 * a12) - a01 * (a01 * c2 - a12 * a02) + a02 * (a01 * a12 - c1 * a02);
+        if (m2 > 0.0f)
+            lmin += dB / m2;
+    }
     const float3 r0 = make_float3(a00 - lmin, a01, a02);
     const float3 r1 = make_float3(a01, a11 - lmin, a12);
     const float3 r2 = make_float3(a02, a12, a22 - lmin);

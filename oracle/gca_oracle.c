@@ -1230,8 +1230,12 @@ void orc_color_icp_f64(const float *sx, const float *srgb, int64_t ns, const flo
     double rr = cell * cell;
     int nthr = g_threads;
     double *part = (double *)calloc((size_t)nthr, sizeof(double) * 48);
+    const float rrf = P->max_corr * P->max_corr;
     for (int it = 0; it < P->max_iter; ++it) {
         memset(part, 0, sizeof(double) * 48 * (size_t)nthr);
+        float tf[12];
+        for (int k = 0; k < 12; ++k)
+            tf[k] = (float)T[k];
 #ifdef _OPENMP
 #pragma omp parallel num_threads(nthr)
 #endif
@@ -1246,14 +1250,25 @@ void orc_color_icp_f64(const float *sx, const float *srgb, int64_t ns, const flo
 #endif
             for (int64_t i = 0; i < ns; ++i) {
                 d3 p0 = d3loadf(sx, i);
-                d3 p = d3m(T[0] * p0.x + T[1] * p0.y + T[2] * p0.z + T[3],
-                           T[4] * p0.x + T[5] * p0.y + T[6] * p0.z + T[7],
-                           T[8] * p0.x + T[9] * p0.y + T[10] * p0.z + T[11]);
+                d3 p;
+                float pf[3] = {0.0f, 0.0f, 0.0f};
+                if (P->search_f32) {
+                    /* the GPU kernels' point: orc_apply_pose_f32 */
+                    for (int r = 0; r < 3; ++r)
+                        pf[r] = fmaf(tf[4 * r], sx[3 * i], fmaf(tf[4 * r + 1], sx[3 * i + 1],
+                                                                fmaf(tf[4 * r + 2], sx[3 * i + 2], tf[4 * r + 3])));
+                    p = d3m(pf[0], pf[1], pf[2]);
+                } else {
+                    p = d3m(T[0] * p0.x + T[1] * p0.y + T[2] * p0.z + T[3],
+                            T[4] * p0.x + T[5] * p0.y + T[6] * p0.z + T[7],
+                            T[8] * p0.x + T[9] * p0.y + T[10] * p0.z + T[11]);
+                }
                 int32_t c[3];
                 c[0] = (int32_t)floor((p.x - (double)gmin[0]) / cell);
                 c[1] = (int32_t)floor((p.y - (double)gmin[1]) / cell);
                 c[2] = (int32_t)floor((p.z - (double)gmin[2]) / cell);
                 double best = rr;
+                float bestf = rrf;
                 int64_t bi = -1;
                 for (int di = -1; di <= 1; ++di)
                     for (int dj = -1; dj <= 1; ++dj)
@@ -1263,6 +1278,17 @@ void orc_color_icp_f64(const float *sx, const float *srgb, int64_t ns, const flo
                                 const vkey *e = &g.cells[s];
                                 if (e->k[0] != x || e->k[1] != y || e->k[2] != z)
                                     break;
+                                if (P->search_f32) {
+                                    /* unfused FP32 d^2 in the reference's order (q - p) */
+                                    const float ex = tx[3 * e->idx] - pf[0], ey = tx[3 * e->idx + 1] - pf[1],
+                                                ez = tx[3 * e->idx + 2] - pf[2];
+                                    const float d2f = ex * ex + ey * ey + ez * ez;
+                                    if (d2f < rrf && (bi < 0 || d2f < bestf || (d2f == bestf && e->idx < bi))) {
+                                        bestf = d2f;
+                                        bi = e->idx;
+                                    }
+                                    continue;
+                                }
                                 d3 q = d3loadf(tx, e->idx);
                                 d3 dd = d3sub(q, p);
                                 double d2 = d3dot(dd, dd);
@@ -1274,6 +1300,8 @@ void orc_color_icp_f64(const float *sx, const float *srgb, int64_t ns, const flo
                         }
                 if (bi < 0)
                     continue;
+                if (P->search_f32)
+                    best = (double)bestf;
                 d3 q = d3loadf(tx, bi);
                 d3 n = d3m(tn[3 * bi], tn[3 * bi + 1], tn[3 * bi + 2]);
                 d3 d = d3m(tg[3 * bi], tg[3 * bi + 1], tg[3 * bi + 2]);

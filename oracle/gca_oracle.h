@@ -127,6 +127,10 @@ typedef struct {
     int update_map;
     double rot_eps;   /* converged when cos(step angle) >= 1 - rot_eps */
     double trans_eps; /* ... and |step t|^2 <= trans_eps */
+    int search_f32;   /* 1: correspondences of the FP32 points the GPU kernels search
+                       * (pose rounded to float, fused x' = fma(r0,x,fma(r1,y,fma(r2,z,t))),
+                       * unfused FP32 d^2 < max_corr^2); residuals, Jacobians and sums
+                       * stay FP64 on those points.  0: FP64 transform and search. */
 } orc_icp_params;
 
 typedef struct {
@@ -140,7 +144,8 @@ typedef struct {
 } orc_icp_result;
 
 /* colored ICP in FP64 (color_icp.cu:151-234 with FP64 everywhere, pose applied on
- * the fly, (distance, index) NN tie-break).  tgt_nrm/tgt_grad are FP64. */
+ * the fly, (distance, index) NN tie-break).  tgt_nrm/tgt_grad are FP64.  With
+ * p->search_f32 the correspondences are those of the FP32 points (above). */
 void orc_color_icp_f64(const float *src_xyz, const float *src_rgb, int64_t ns,
                        const float *tgt_xyz, const float *tgt_rgb, const double *tgt_nrm,
                        const double *tgt_grad, int64_t nt, const orc_icp_params *p,

@@ -55,7 +55,8 @@ class Extrinsics(C.Structure):
 
 class IcpParams(C.Structure):
     _fields_ = [("max_iter", C.c_int), ("max_corr", C.c_float), ("lambda_", C.c_float),
-                ("update_map", C.c_int), ("rot_eps", C.c_double), ("trans_eps", C.c_double)]
+                ("update_map", C.c_int), ("rot_eps", C.c_double), ("trans_eps", C.c_double),
+                ("search_f32", C.c_int)]
 
 
 class UnrollParams(C.Structure):
@@ -289,8 +290,13 @@ def _icp_out(r):
 
 
 def color_icp_f64(src_xyz, src_rgb, tgt_xyz, tgt_rgb, tgt_nrm, tgt_grad, max_iter=30, max_corr=0.03,
-                  lam=0.968, update_map=UPDATE_EULER_ZYX, rot_eps=1e-6, trans_eps=1e-6, T_init=None):
-    p = IcpParams(int(max_iter), float(max_corr), float(lam), int(update_map), float(rot_eps), float(trans_eps))
+                  lam=0.968, update_map=UPDATE_EULER_ZYX, rot_eps=1e-6, trans_eps=1e-6, T_init=None,
+                  search_f32=False):
+    """search_f32: correspondences of the FP32 points that the GPU kernels search
+    (pose rounded to float, fused application, FP32 squared distances); residuals,
+    Jacobians, sums and the solve stay FP64"""
+    p = IcpParams(int(max_iter), float(max_corr), float(lam), int(update_map), float(rot_eps), float(trans_eps),
+                  int(bool(search_f32)))
     T0 = np.eye(4) if T_init is None else np.asarray(T_init, np.float64)
     r = IcpResult()
     lib().orc_color_icp_f64(_f32(src_xyz), _f32(src_rgb), len(src_xyz), _f32(tgt_xyz), _f32(tgt_rgb),
@@ -327,7 +333,7 @@ class Scale:
 
 
 def multiscale_f64(src_xyz, src_rgb, tgt_xyz, tgt_rgb, scales, lam=0.968, update_map=UPDATE_SE3_EXP,
-                   rot_eps=1e-6, trans_eps=1e-6, T_init=None):
+                   rot_eps=1e-6, trans_eps=1e-6, T_init=None, search_f32=False):
     T = np.eye(4) if T_init is None else np.asarray(T_init, np.float64)
     results = []
     for s in scales:
@@ -335,7 +341,8 @@ def multiscale_f64(src_xyz, src_rgb, tgt_xyz, tgt_rgb, scales, lam=0.968, update
         tx, tc, _, _ = voxel_downsample(tgt_xyz, tgt_rgb, s.voxel)
         tn = normals_f64(tx, s.normal_radius, s.max_nn)
         tg = gradient_f64(tx, tc, tn, s.grad_radius)
-        r = color_icp_f64(sx, sc, tx, tc, tn, tg, s.iters, s.max_corr, lam, update_map, rot_eps, trans_eps, T)
+        r = color_icp_f64(sx, sc, tx, tc, tn, tg, s.iters, s.max_corr, lam, update_map, rot_eps, trans_eps, T,
+                          search_f32)
         T = r.T
         results.append(r)
     return T, results

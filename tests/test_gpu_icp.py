@@ -71,7 +71,8 @@ def test_icp_plain_and_compensated_agree(ctx, N, synth, pair_c1):
     rc = run_gpu(ctx, N, pair_c1, c1_scales(N), update_map=N.UPDATE_SE3_EXP, compensated=True)
     rp = run_gpu(ctx, N, pair_c1, c1_scales(N), update_map=N.UPDATE_SE3_EXP, compensated=False)
     rot, tr = synth.pose_error(rc["T"], rp["T"])
-    assert rot < 1e-4 and tr < 1e-4
+    assert rot <= POSE_TOL and tr <= POSE_TOL, (rot, tr)
+    assert rc["scale_iterations"] == rp["scale_iterations"]
 
 
 def test_icp_reference_single_level_align(ctx, N, orc, synth):

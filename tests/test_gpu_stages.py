@@ -34,9 +34,11 @@ def room():
 
 
 def angle_err(a, b):
+    """unsigned angle between line directions, atan2(|a x b|, |a . b|): arccos of a
+    dot product near 1 reads sqrt(2 delta) for a rounding delta of the norms"""
     a = a / np.maximum(np.linalg.norm(a, axis=1, keepdims=True), 1e-30)
     b = b / np.maximum(np.linalg.norm(b, axis=1, keepdims=True), 1e-30)
-    return np.arccos(np.clip(np.abs((a * b).sum(1)), -1, 1))
+    return np.arctan2(np.linalg.norm(np.cross(a, b), axis=1), np.abs((a * b).sum(1)))
 
 
 # --------------------------------------------------------------------------- #
@@ -109,6 +111,35 @@ def test_upload_many_matches_single_uploads(ctx, N, golden):
         d = c.download()
         np.testing.assert_array_equal(d["xyz"], w["xyz"])
         np.testing.assert_array_equal(d["rgb"], w["rgb"])
+
+
+def test_upload_many_repeated_cloud_keeps_call_order(ctx, N, golden):
+    """A cloud named several times in one call ends with its last entry, whatever the
+    sources of the entries (in place or staged)."""
+    torch = pytest.importorskip("torch")
+    xyz, rgb = golden["cloud_xyz"], golden["cloud_rgb"]
+    n = len(xyz)
+    pinned = [torch.from_numpy(np.ascontiguousarray(a, np.float32)).pin_memory() for a in (xyz, rgb)]
+    pageable = [np.ascontiguousarray(a, np.float32) for a in (xyz, rgb)]
+    pin = lambda off: (pinned[0].data_ptr() + 12 * off, pinned[1].data_ptr() + 12 * off)
+    page = lambda off: (pageable[0].ctypes.data + 12 * off, pageable[1].ctypes.data + 12 * off)
+    # (source, first point, count) per entry, all into one cloud; the last entry wins
+    for seq in ([(pin, 0, 500), (page, 10, 300)], [(page, 10, 300), (pin, 0, 500)],
+                [(pin, 0, 500), (pin, 20, 200)], [(pin, 0, 500), (page, 3, 50), (pin, 40, 400)]):
+        c = N.Cloud(ctx, n)
+        xp, rp, cnt = [], [], []
+        for src, off, m in seq:
+            a, b = src(off)
+            xp.append(a)
+            rp.append(b)
+            cnt.append(m)
+        N.upload_many(ctx, [c] * len(seq), xp, rp, cnt)
+        _, off, m = seq[-1]
+        ref = ctx.cloud_from(xyz[off:off + m], rgb[off:off + m])
+        want, got = ref.download(), c.download()
+        assert len(c) == m
+        np.testing.assert_array_equal(got["xyz"], want["xyz"])
+        np.testing.assert_array_equal(got["rgb"], want["rgb"])
 
 
 def test_bounds_true_max(ctx, golden):
@@ -268,9 +299,13 @@ def test_normals_vs_f64(ctx, orc, room_v01, max_nn):
     np.testing.assert_array_equal(zero_g, zero_r)
     ok = ~zero_r
     err = angle_err(n[ok].astype(np.float64), ref[ok])
-    # well-conditioned points match to 1e-3 rad; the sign follows n_z <= 0
-    assert np.percentile(err, 99) < 1e-3, np.percentile(err, [50, 99, 100])
-    assert np.median(err) < 1e-5
+    # FP32 moments and closed form (Newton-refined smallest eigenvalue); the points
+    # whose relative eigenvalue gap is below 1e-3 come from the FP64 pass.  Just above
+    # that gap the FP32 covariance's own rounding (a few eps of its largest entry)
+    # bounds the angle at about 1e-6 / gap.  The sign follows n_z <= 0.
+    assert np.median(err) < 1e-6, np.percentile(err, [50, 99, 100])
+    assert np.percentile(err, 99) < 1e-4, np.percentile(err, [50, 99, 100])
+    assert err.max() < 2e-3, np.percentile(err, [50, 99, 100])
     sign_ok = (n[ok, 2] <= 0) | (np.abs(n[ok, 2]) < 1e-6)
     assert sign_ok.all()
     np.testing.assert_allclose(np.linalg.norm(n[ok], axis=1), 1.0, atol=1e-5)
