@@ -18,6 +18,10 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgca3d.so")
 OBJDIR = os.path.join(LIBDIR, "obj")
+# the checked build: device-side index checks compiled in (GCA3D_CHECKED), each failure
+# a status (an error bit of the context), never a fault or a trap; same entry points
+LIB_CHECKED = os.path.join(LIBDIR, "libgca3d_checked.so")
+OBJDIR_CHECKED = os.path.join(LIBDIR, "obj_checked")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include"),
@@ -35,8 +39,8 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _compile(src, extra):
-    obj = os.path.join(OBJDIR, os.path.basename(src)[:-3] + ".o")
+def _compile(src, extra, objdir=OBJDIR):
+    obj = os.path.join(objdir, os.path.basename(src)[:-3] + ".o")
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -44,32 +48,35 @@ def _compile(src, extra):
     return obj
 
 
-def _stale():
-    if not os.path.exists(LIB):
+def _stale(lib=LIB):
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
     deps.append(os.path.join(ROOT, "include", "gca3d.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, extra=(), verbose=False):
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OBJDIR, exist_ok=True)
+def build(force=False, extra=(), verbose=False, checked=False):
+    """libgca3d.so, or with checked=True libgca3d_checked.so (index checks compiled in)"""
+    lib, objdir = (LIB_CHECKED, OBJDIR_CHECKED) if checked else (LIB, OBJDIR)
+    extra = list(extra) + (["-DGCA3D_CHECKED"] if checked else [])
+    if not force and not _stale(lib):
+        return lib
+    os.makedirs(objdir, exist_ok=True)
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, extra, objdir), srcs))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-ldl", "-lpthread", "-lrt"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
-        print(f"built {LIB}")
-    return LIB
+        print(f"built {lib}")
+    return lib
 
 
 if __name__ == "__main__":

@@ -90,6 +90,8 @@ int consume_device_error(gca3d_context *ctx, const char *where)
         return fail(ctx, GCA3D_ERR_CAPACITY, std::string(where) + ": output capacity exceeded");
     if (h & kErrInvalid)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, std::string(where) + ": invalid value on the device");
+    if (h & kErrBounds)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, std::string(where) + ": an index check failed (checked build)");
     return GCA3D_OK;
 }
 
@@ -374,13 +376,16 @@ int gca3d_create(int device, void *stream, gca3d_context **out)
         }
         ctx->own_stream = true;
     }
-    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess ||
+    if (cudaMalloc(&ctx->d_err, 2 * sizeof(int)) != cudaSuccess ||
         cudaMallocHost(&ctx->h_pinned, 64 * sizeof(int)) != cudaSuccess)
     {
         gca3d_destroy(ctx);
         return GCA3D_ERR_OUT_OF_MEMORY;
     }
-    cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream);
+    ctx->h_pinned[0] = 0;
+    ctx->h_pinned[1] = kWaitLimitDefault;
+    cudaMemcpyAsync(ctx->d_err, ctx->h_pinned, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
     *out = ctx;
     return GCA3D_OK;
 }
@@ -411,6 +416,30 @@ int gca3d_synchronize(gca3d_context *ctx)
         return GCA3D_ERR_INVALID_VALUE;
     GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return consume_device_error(ctx, "synchronize");
+}
+
+int gca3d_set_wait_limit(gca3d_context *ctx, int polls)
+{
+    if (!ctx || polls < 1)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "set_wait_limit: polls must be >= 1");
+    cudaSetDevice(ctx->device);
+    ctx->h_pinned[63] = polls;
+    GCA_CUDA(ctx, cudaMemcpyAsync(ctx->d_err + 1, ctx->h_pinned + 63, sizeof(int), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GCA3D_OK;
+}
+
+int gca3d_get_wait_limit(gca3d_context *ctx, int *polls)
+{
+    if (!ctx || !polls)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "get_wait_limit: bad arguments");
+    cudaSetDevice(ctx->device);
+    GCA_CUDA(ctx, cudaMemcpyAsync(ctx->h_pinned + 63, ctx->d_err + 1, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *polls = ctx->h_pinned[63];
+    return GCA3D_OK;
 }
 
 const char *gca3d_last_error(gca3d_context *ctx)

@@ -230,11 +230,12 @@ __global__ void __launch_bounds__(kFrameThreads) k_frame(const uint16_t *__restr
                 unsigned long long s = kRowInc; // above row 0: an inclusive zero
                 if (p >= 0)
                 {
+                    const uint32_t limit = wait_limit(d_err);
                     unsigned spins = 0;
                     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(s) : "l"(status + p) : "memory");
                     while ((s & kRowFlag) == 0)
                     {
-                        if (++spins > kSpinLimit)
+                        if (++spins > limit)
                         {
                             atomicOr(d_err, kErrTimeout);
                             break; // a state that never came counts as the end of the look-back

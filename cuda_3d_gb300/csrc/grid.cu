@@ -97,7 +97,7 @@ __global__ void k_grid_keys(const float4 *__restrict__ pos, const int32_t *seg_o
 }
 
 __global__ void k_grid_scatter(SortBuffers sb, const int32_t *d_n, const KeyLayout *lay, const float4 *__restrict__ pos,
-                               float4 *spos, int32_t *sidx, float *sint, int *scz, uint64_t *skey)
+                               float4 *spos, int32_t *sidx, float *sint, int *scz, uint64_t *skey, int *err)
 {
     const int n = *d_n;
     const uint64_t *keys = sb.keys[*sb.d_sel];
@@ -108,6 +108,8 @@ __global__ void k_grid_scatter(SortBuffers sb, const int32_t *d_n, const KeyLayo
     {
         uint64_t k = keys[s];
         int g = vals[s];
+        if (!GCA_INDEX_OK(g, n, err))
+            continue;
         float4 p = pos[g];
         spos[s] = make_float4(p.x, p.y, p.z, __int_as_float((int)(k & mz)));
         sidx[s] = g;
@@ -194,6 +196,8 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     d.slots = A.get<RowSlot>(hcap);
     d.hmask = hcap - 1;
     d.seg_off = b.seg_off;
+    d.d_n = b.seg_off + P;
+    d.err = ctx->d_err;
     int *ord = A.get<int>(6 * P);
     SortBuffers sb;
     sb.keys[0] = A.get<uint64_t>(cap);
@@ -220,7 +224,7 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
         return st;
     const int gs = std::min(grid_for(cap), ctx->num_sms * 8);
     GCA_PROF_BEGIN(ctx, kKidGridScatter);
-    k_grid_scatter<<<gs, kBlock, 0, s>>>(sb, d_n, d.layout, b.pos, d.spos, d.sidx, d.sint, d.scz, d.skey);
+    k_grid_scatter<<<gs, kBlock, 0, s>>>(sb, d_n, d.layout, b.pos, d.spos, d.sidx, d.sint, d.scz, d.skey, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidGridScatter);
     GCA_CUDA(ctx, cudaMemsetAsync(d.slots, 0xFF, sizeof(RowSlot) * hcap, s));

@@ -91,6 +91,8 @@ __device__ __forceinline__ void row_scan(const GridDev &g, int t, int e, int lo,
 {
     if (t >= e)
         return;
+    if (!GCA_INDEX_OK(t, *g.d_n, g.err) || !GCA_INDEX_OK(e - 1, *g.d_n, g.err))
+        return;
     if (e - t > 8)
         t = row_seek_z(g.scz, t, e, lo);
     for (bool more = true; more && t < e; t += Batch)

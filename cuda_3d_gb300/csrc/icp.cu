@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(kIcpThreads, 3) k_icp_accum(const float4 *__re
                                                            const float4 *__restrict__ attr1,
                                                            const int2 *__restrict__ corr, const PairState *st,
                                                            const int *bmap, int P, double *partials, float slg,
-                                                           float slc)
+                                                           float slc, const int32_t *d_nt, int *err)
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
@@ -464,6 +464,8 @@ __global__ void __launch_bounds__(kIcpThreads, 3) k_icp_accum(const float4 *__re
         {
             const int i = b.start + (int)threadIdx.x + kIcpThreads * (j0 + j);
             c[j] = i < b.end ? corr[i] : make_int2(-1, 0);
+            if (c[j].x >= 0 && !GCA_INDEX_OK(c[j].x, *d_nt, err))
+                c[j].x = -1;
             if (c[j].x >= 0)
             {
                 s4[j] = src_pos[i];
@@ -752,11 +754,11 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
     if (compensated)
         k_icp_accum<true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
                                                                      corr, st, bmap, src.P, partials, prm.sqrt_lg,
-                                                                     prm.sqrt_lc);
+                                                                     prm.sqrt_lc, g.dev.d_n, ctx->d_err);
     else
         k_icp_accum<false><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
                                                                       corr, st, bmap, src.P, partials, prm.sqrt_lg,
-                                                                      prm.sqrt_lc);
+                                                                      prm.sqrt_lc, g.dev.d_n, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     if (compensated)
         k_icp_finalize<true><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm, loop);
@@ -775,9 +777,11 @@ __global__ void __launch_bounds__(kIcpThreads) k_build_gn(const float4 *__restri
                                                           const float4 *__restrict__ tp, const float4 *__restrict__ tn,
                                                           const float4 *__restrict__ tg, const int32_t *nn,
                                                           float slg, float slc, double *partials,
-                                                          unsigned *ticket, double *out)
+                                                          unsigned *ticket, double *out, const int32_t *d_nt,
+                                                          int *d_err)
 {
     const int ns = *d_ns;
+    const int nt = d_nt ? *d_nt : INT_MAX;
     Acc<true> acc;
     acc.zero();
     for (int i = blockIdx.x * kIcpThreads + threadIdx.x; i < ns; i += gridDim.x * kIcpThreads)
@@ -785,6 +789,11 @@ __global__ void __launch_bounds__(kIcpThreads) k_build_gn(const float4 *__restri
         const int j = nn[i];
         if (j < 0)
             continue;
+        if (j >= nt)
+        {
+            atomicOr(d_err, kErrInvalid);
+            continue;
+        }
         const float4 s4 = sp[i], q = tp[j], n = tn[j], d = tg[j];
         GNTerms t;
         gn_terms(make_float3(s4.x, s4.y, s4.z), s4.w, make_float3(q.x, q.y, q.z), q.w, make_float3(n.x, n.y, n.z),
@@ -814,14 +823,17 @@ __global__ void __launch_bounds__(kIcpThreads) k_build_gn(const float4 *__restri
 
 __global__ void k_abs_residual(const float4 *__restrict__ sp, const int32_t *d_ns, const float4 *__restrict__ tp,
                                const float4 *__restrict__ tn, const float4 *__restrict__ tg, const int32_t *nn,
-                               float slg, float slc, float *out)
+                               float slg, float slc, float *out, const int32_t *d_nt, int *d_err)
 {
     const int ns = *d_ns;
+    const int nt = *d_nt;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x)
     {
         const int j = nn[i];
-        if (j < 0)
+        if (j < 0 || j >= nt)
         {
+            if (j >= nt)
+                atomicOr(d_err, kErrInvalid); // an index beyond the target
             out[i] = 0.0f;
             continue;
         }
@@ -844,20 +856,22 @@ int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt,
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "build_gn: scratch");
     GCA_CUDA(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream));
     k_build_gn<<<blocks, kIcpThreads, 0, ctx->stream>>>(src->pos, src->d_count, tgt->pos, tgt->nrm, tgt->grd, nn,
-                                                        sqrtf(lambda), sqrtf(1.0f - lambda), partials, ticket, d_out);
+                                                        sqrtf(lambda), sqrtf(1.0f - lambda), partials, ticket, d_out,
+                                                        tgt->d_count, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     GCA_CUDA(ctx, cudaMemcpyAsync(out30, d_out, sizeof(double) * kTerms, cudaMemcpyDeviceToHost, ctx->stream));
     GCA_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return GCA3D_OK;
+    return consume_device_error(ctx, "build_gauss_newton: a correspondence index lies beyond the target");
 }
 
 int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
                  float *out)
 {
     k_abs_residual<<<grid_for(src->capacity), kBlock, 0, ctx->stream>>>(
-        src->pos, src->d_count, tgt->pos, tgt->nrm, tgt->grd, nn, sqrtf(lambda), sqrtf(1.0f - lambda), out);
+        src->pos, src->d_count, tgt->pos, tgt->nrm, tgt->grd, nn, sqrtf(lambda), sqrtf(1.0f - lambda), out,
+        tgt->d_count, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
-    return GCA3D_OK;
+    return consume_device_error(ctx, "abs_residual: a correspondence index lies beyond the target");
 }
 
 } // namespace gca3d

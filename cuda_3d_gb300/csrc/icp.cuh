@@ -78,11 +78,13 @@ struct IcpLoop
 };
 
 // the Gauss-Newton system for given correspondences (defined in icp.cu); the block
-// partials, the ticket and the count are scratch supplied by the caller
+// partials, the ticket and the count are scratch supplied by the caller.  With d_nt
+// (the target count) an index at or beyond it is skipped and recorded as kErrInvalid
+// in *d_err; without it the indices must lie inside the target.
 __global__ void __launch_bounds__(kIcpThreads)
     k_build_gn(const float4 *__restrict__ sp, const int32_t *d_ns, const float4 *__restrict__ tp,
                const float4 *__restrict__ tn, const float4 *__restrict__ tg, const int32_t *nn, float slg, float slc,
-               double *partials, unsigned *ticket, double *out);
+               double *partials, unsigned *ticket, double *out, const int32_t *d_nt, int *d_err);
 
 int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tinit);
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,

@@ -18,7 +18,7 @@ namespace gca3d
 // ---------------------------------------------------------------------------
 constexpr int kMaxSegments = 4096;       // pairs / clouds in one batched stage
 constexpr int kBlock = 256;              // threads per block for streaming kernels
-constexpr uint32_t kSpinLimit = 1u << 22; // polls before a look-back gives up
+constexpr int kWaitLimitDefault = 1 << 22; // polls before a cross-block wait gives up (about 0.3 s)
 
 // device error word bits
 enum : int
@@ -28,7 +28,18 @@ enum : int
     kErrKeyBits = 4,
     kErrSingular = 8,
     kErrInvalid = 16,
+    kErrBounds = 32, // an index check of the checked build failed
 };
+
+// Index checks of the checked build (compiled with -DGCA3D_CHECKED, the library
+// libgca3d_checked.so): an index outside [0, n) sets kErrBounds in the context's error
+// word and the access is skipped, so a bad index becomes a status, never a fault or a
+// trap.  In the regular build the checks compile to nothing (n is not evaluated).
+#ifdef GCA3D_CHECKED
+#define GCA_INDEX_OK(i, n, err) ::gca3d::index_ok((long long)(i), (long long)(n), (err))
+#else
+#define GCA_INDEX_OK(i, n, err) true
+#endif
 
 // ---------------------------------------------------------------------------
 // scratch memory: chunked bump allocator, reset per top-level call.  A replay
@@ -103,7 +114,10 @@ struct gca3d_context
     bool own_stream = false;
     int num_sms = 0;
     gca3d::Arena arena;
-    int *d_err = nullptr;  // device error word
+    // device control words: [0] error bits (kErr*, set with atomicOr by kernels and
+    // consumed by the host), [1] polls after which a cross-block wait gives up
+    // (gca3d_set_wait_limit; kernels read it when they start)
+    int *d_err = nullptr;
     int *h_pinned = nullptr; // pinned scratch for small read-backs (64 ints)
     int64_t launches = 0;
     std::string last_error;
@@ -243,6 +257,20 @@ template <typename T> __device__ __forceinline__ T warp_sum(T v)
     return v;
 }
 
+// the wait limit of the context whose control words ctl points to (see gca3d_context)
+__device__ __forceinline__ uint32_t wait_limit(const int *ctl)
+{
+    return (uint32_t)*(const volatile int *)(ctl + 1);
+}
+
+__device__ __forceinline__ bool index_ok(long long i, long long n, int *err)
+{
+    if (i >= 0 && i < n)
+        return true;
+    atomicOr(err, kErrBounds);
+    return false;
+}
+
 // bounded spin read of a volatile 64-bit status word until pred holds
 __device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long *p)
 {
@@ -295,6 +323,8 @@ struct GridDev
     RowSlot *slots;
     uint32_t hmask;
     const int32_t *seg_off; // [P + 1] offsets of the segments in the sorted arrays
+    const int32_t *d_n;     // points in the grid (seg_off[P])
+    int *err;               // the context's error word (index checks of the checked build)
 };
 
 constexpr unsigned long long kEmptyKey = ~0ull;

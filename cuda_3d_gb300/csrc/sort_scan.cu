@@ -6,9 +6,11 @@
 // it is stable, so equal keys keep ascending input (original index) order, which is
 // the order the voxel sums and the neighbour scans are defined in.
 //
-// Every look-back wait is bounded: after kSpinLimit polls the kernel records
-// kErrTimeout in the context's error word and continues, so a scheduling fault
-// shows up as a status, never as a hung GPU.
+// Every look-back wait is bounded: after the context's wait limit (polls, read from its
+// control words when the kernel starts) the kernel records kErrTimeout in the context's
+// error word and treats the missing state as the end of its look-back -- the partial
+// prefix only lowers the offsets it writes, which stay inside the output -- so a
+// scheduling fault shows up as a status, never as a hung GPU.
 #include "internal.cuh"
 
 namespace gca3d
@@ -269,6 +271,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
         // the predecessors' states for this digit, kLookWindow at a time (independent
         // relaxed loads), consumed nearest first up to the nearest inclusive one
         bool found = false;
+        const uint32_t limit = wait_limit(d_err);
         for (int64_t p = (int64_t)tile - 1; p >= 0 && !found; p -= kLookWindow)
         {
             uint32_t s[kLookWindow];
@@ -283,7 +286,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
                 uint32_t spins = 0;
                 while ((s[j] & kFlagMask) == 0)
                 {
-                    if (++spins > kSpinLimit)
+                    if (++spins > limit)
                     {
                         atomicOr(d_err, kErrTimeout);
                         break;
@@ -307,6 +310,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
         uint64_t kk = s_keys[j];
         uint32_t d = (uint32_t)(kk >> shift) & 255u;
         uint32_t g = s_gbase[d] + j;
+        if (!GCA_INDEX_OK(g, n, d_err))
+            continue;
         kout[g] = kk;
         vout[g] = s_vals[j];
     }
@@ -423,11 +428,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict
                 unsigned long long s = kSFlagInc; // before tile 0: an inclusive zero
                 if (p >= 0)
                 {
+                    const uint32_t limit = wait_limit(d_err);
                     uint32_t spins = 0;
                     s = ld_acquire64(status + p);
                     while ((s & kSFlagMask) == 0)
                     {
-                        if (++spins > kSpinLimit)
+                        if (++spins > limit)
                         {
                             atomicOr(d_err, kErrTimeout);
                             break;
@@ -488,3 +494,62 @@ int exclusive_scan(gca3d_context *ctx, const int32_t *in, int32_t *out, const in
 }
 
 } // namespace gca3d
+
+using namespace gca3d;
+
+// A scan of `tiles` tiles launched with tiles - 1 blocks whose tile ticket starts at 1:
+// tile 0 is never run, so status[0] is never published and tile 1's look-back waits
+// on it until the wait limit; the later tiles wait on tile 1, which publishes after
+// giving up.  Every block's tile lies in [1, tiles), every read and write inside the
+// tiles * kScanTile inputs and outputs and the tiles status words.
+int gca3d_selfcheck_wait(gca3d_context *ctx, int tiles, int polls, int *wait_status, double *elapsed_ms)
+{
+    if (!ctx || tiles < 2 || tiles > 64 || polls < 1 || !wait_status)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "selfcheck_wait: tiles in 2..64, polls >= 1");
+    cudaSetDevice(ctx->device);
+    int old_limit = 0;
+    int st = gca3d_get_wait_limit(ctx, &old_limit);
+    if (st)
+        return st;
+    consume_device_error(ctx, "selfcheck_wait"); // start from a clear error word
+    ctx->arena.reset();
+    const int n = tiles * kScanTile;
+    int32_t *in = ctx->arena.get<int32_t>(n), *out = ctx->arena.get<int32_t>(n);
+    int32_t *d_n = ctx->arena.get<int32_t>(1);
+    ScanCtl *ctl = ctx->arena.get<ScanCtl>(1);
+    unsigned long long *status = ctx->arena.get<unsigned long long>(tiles);
+    if (!in || !out || !d_n || !ctl || !status)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "selfcheck_wait: scratch");
+    GCA_CUDA(ctx, cudaMemsetAsync(in, 0, sizeof(int32_t) * n, ctx->stream));
+    GCA_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(unsigned long long) * tiles, ctx->stream));
+    ctx->h_pinned[60] = n;
+    ctx->h_pinned[61] = 1; // first ticket
+    GCA_CUDA(ctx, cudaMemcpyAsync(d_n, ctx->h_pinned + 60, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    GCA_CUDA(ctx, cudaMemcpyAsync(&ctl->tile_ctr, ctx->h_pinned + 61, sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    st = gca3d_set_wait_limit(ctx, polls);
+    if (st)
+        return st;
+    cudaEvent_t e0, e1;
+    GCA_CUDA(ctx, cudaEventCreate(&e0));
+    GCA_CUDA(ctx, cudaEventCreate(&e1));
+    cudaEventRecord(e0, ctx->stream);
+    k_scan<<<tiles - 1, kScanThreads, 0, ctx->stream>>>(in, out, d_n, ctl, status, nullptr, ctx->d_err);
+    const cudaError_t le = cudaGetLastError();
+    ctx->launches++;
+    cudaEventRecord(e1, ctx->stream);
+    const cudaError_t se = cudaStreamSynchronize(ctx->stream);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (elapsed_ms)
+        *elapsed_ms = ms;
+    *wait_status = consume_device_error(ctx, "selfcheck_wait: scan");
+    const int rs = gca3d_set_wait_limit(ctx, old_limit);
+    if (le != cudaSuccess)
+        return cuda_fail(ctx, le, "selfcheck_wait: launch");
+    if (se != cudaSuccess)
+        return cuda_fail(ctx, se, "selfcheck_wait: synchronize");
+    return rs;
+}

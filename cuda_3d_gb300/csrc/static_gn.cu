@@ -116,7 +116,7 @@ extern "C" int gca3d_build_gauss_newton_static(void *stream, const void *src_pos
     k_build_gn<<<blocks, kIcpThreads, 0, cs>>>(
         static_cast<const float4 *>(src_pos), &s->n_src, static_cast<const float4 *>(tgt_pos),
         static_cast<const float4 *>(tgt_nrm), static_cast<const float4 *>(tgt_grd), nn, sqrtf(lambda),
-        sqrtf(1.0f - lambda), s->partials, &s->ticket, s->out);
+        sqrtf(1.0f - lambda), s->partials, &s->ticket, s->out, nullptr, nullptr);
     k_static_expand<<<1, 64, 0, cs>>>(s, jtj, jtr, r2);
     if (cudaGetLastError() != cudaSuccess)
         return GCA3D_ERR_CUDA;

@@ -229,7 +229,7 @@ __global__ void k_seg_first_to_offsets(const int32_t *seg_first, int P, const in
 }
 
 __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuffers sb, const int32_t *starts,
-                               const int32_t *d_m, const KeyLayout *lay, float4 *opos, float4 *ocol)
+                               const int32_t *d_m, const KeyLayout *lay, float4 *opos, float4 *ocol, int *err)
 {
     const int m = *d_m;
     const uint64_t *keys = sb.keys[*sb.d_sel];
@@ -244,11 +244,15 @@ __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuf
         const float4 *ps = src[seg].pos;
         const float4 *cs = src[seg].col;
         int g = vals[s] - base;
+        if (!GCA_INDEX_OK(g, in_off[seg + 1] - base, err))
+            continue;
         float4 p = ps[g], c = cs[g];
         float sx = p.x, sy = p.y, sz = p.z, cr = c.x, cg = c.y, cb = c.z;
         for (int j = s + 1; j < e; ++j)
         {
             g = vals[j] - base;
+            if (!GCA_INDEX_OK(g, in_off[seg + 1] - base, err))
+                break;
             p = ps[g];
             c = cs[g];
             sx = __fadd_rn(sx, p.x);
@@ -323,7 +327,7 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts, sb, lay, seg_count);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_BEGIN(ctx, kKidVoxelReduce);
-    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col);
+    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_END(ctx, kKidVoxelReduce);
     k_seg_first_to_offsets<<<1, 32, 0, s>>>(seg_count, P, d_m, out.seg_off);

@@ -151,11 +151,14 @@ _SIGS = {
     "gca3d_color_icp_vjp": [_P, _P, _P, C.POINTER(VjpParams), _P, _P, C.c_double, _P, C.POINTER(C.c_double), _P,
                             _P, _P, _P],
     "gca3d_selfcheck_fp64": [_P, C.c_int, _P],
+    "gca3d_set_wait_limit": [_P, C.c_int],
+    "gca3d_get_wait_limit": [_P, C.POINTER(C.c_int)],
+    "gca3d_selfcheck_wait": [_P, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)],
 }
 _RESTYPES = {"gca3d_status_string": C.c_char_p, "gca3d_last_error": C.c_char_p,
              "gca3d_kernel_launches": C.c_int64, "gca3d_stream": C.c_void_p}
 
-_lib = None
+_lib = {}
 
 
 def exported_symbols():
@@ -164,10 +167,10 @@ def exported_symbols():
 
 
 def load(path=LIB_PATH):
-    """load libgca3d.so (raises if it was not built)"""
-    global _lib
-    if _lib is not None:
-        return _lib
+    """load libgca3d.so, or another build of it such as libgca3d_checked.so (raises if
+    it was not built)"""
+    if path in _lib:
+        return _lib[path]
     if not os.path.exists(path):
         raise RuntimeError(f"{path} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
     L = C.CDLL(path)
@@ -175,7 +178,7 @@ def load(path=LIB_PATH):
         f = getattr(L, name)
         f.argtypes = args
         f.restype = _RESTYPES.get(name, C.c_int)
-    _lib = L
+    _lib[path] = L
     return L
 
 
@@ -190,10 +193,11 @@ def _ptr(a):
 
 
 class Context:
-    """owns a gca3d_context; stream=None creates a private non-blocking stream"""
+    """owns a gca3d_context; stream=None creates a private non-blocking stream;
+    lib_path selects another build of the library (the checked build)"""
 
-    def __init__(self, device=0, stream=None):
-        self.L = load()
+    def __init__(self, device=0, stream=None, lib_path=LIB_PATH):
+        self.L = load(lib_path)
         h = C.c_void_p()
         st = self.L.gca3d_create(device, stream, C.byref(h))
         if st != OK:
@@ -432,6 +436,23 @@ def selfcheck_fp64(ctx, n=1 << 20):
     ctx.check(ctx.L.gca3d_selfcheck_fp64(ctx.h, int(n), out.ctypes.data_as(C.c_void_p)))
     return {"rcp_ulp": float(out[0]), "sin_ulp": float(out[1]), "cos_ulp": float(out[2]),
             "exp_coeff_vs_bound": float(out[3])}
+
+
+def selfcheck_wait(ctx, tiles=8, polls=1000):
+    """run a look-back whose predecessor never publishes: (status the scan reported,
+    its duration in ms)"""
+    st, ms = C.c_int(), C.c_double()
+    ctx.check(ctx.L.gca3d_selfcheck_wait(ctx.h, int(tiles), int(polls), C.byref(st), C.byref(ms)))
+    return st.value, ms.value
+
+
+def wait_limit(ctx, polls=None):
+    """the context's wait limit in polls; sets it first when polls is given"""
+    if polls is not None:
+        ctx.check(ctx.L.gca3d_set_wait_limit(ctx.h, int(polls)))
+    v = C.c_int()
+    ctx.check(ctx.L.gca3d_get_wait_limit(ctx.h, C.byref(v)))
+    return v.value
 
 
 def color_icp_vjp(ctx, src, tgt, xi0, K=5, max_corr=0.05, lam=0.968, update_map=UPDATE_SE3_EXP, dT=None, dE=0.0,

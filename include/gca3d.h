@@ -442,6 +442,26 @@ int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt,
  * ------------------------------------------------------------------------- */
 int gca3d_selfcheck_fp64(gca3d_context *ctx, int n, double out[4]);
 
+/* ---------------------------------------------------------------------------
+ * bounded cross-block waits (no reference counterpart: the reference's kernels
+ * never wait on one another).  The look-backs of the radix sort, the scan and the
+ * frame compaction poll their predecessors' states; after `polls` unanswered
+ * polls (64 ns sleeps between them after the first 64) a wait gives up, the
+ * state counts as the end of the look-back (offsets stay inside the outputs) and
+ * the call returns GCA3D_ERR_TIMEOUT.  Default 4,194,304 polls (about 0.3 s).
+ * The limit is read by the kernels when they run, so it also applies to graphs
+ * captured before it was set.  polls >= 1.
+ * ------------------------------------------------------------------------- */
+int gca3d_set_wait_limit(gca3d_context *ctx, int polls);
+int gca3d_get_wait_limit(gca3d_context *ctx, int *polls);
+
+/* self-check of the bounded waits: a scan over `tiles` tiles (2..64) whose first
+ * tile is never run, so its successor's look-back waits on a state that never
+ * comes; the wait limit is `polls` for this call.  *wait_status receives the status
+ * the scan's call reports (GCA3D_ERR_TIMEOUT when the wait gave up), *elapsed_ms its
+ * duration on the context stream.  The context stays usable afterwards. */
+int gca3d_selfcheck_wait(gca3d_context *ctx, int tiles, int polls, int *wait_status, double *elapsed_ms);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,7 @@
  * so that its results are reproducible on x86-64 and aarch64 alike.
  */
 #include "gca_oracle.h"
+#include "det_expf.h"
 
 #include <float.h>
 #include <math.h>
@@ -93,36 +94,9 @@ void orc_aabb(const float *xyz, int64_t n, int flt_min_bug, float mn[3], float m
 /* a1-a3: depth filter + back-projection                               */
 /* ------------------------------------------------------------------ */
 
-/* exp(x) in FP32 by Cody-Waite range reduction (x = k ln2 + r, |r| <= ln2/2, ln2
- * split in a 16-bit head and a tail so k * head is exact) and a degree-7 Taylor
- * polynomial in Horner form, scaled by 2^k in two exact steps.  Plain IEEE
- * multiply/add only, so the CUDA kernel evaluates the identical sequence and the
- * filtered depths agree bit for bit; at most 2 ulp from exp(x). */
-static float orc_expf(float x)
-{
-    if (x != x)
-        return x;
-    if (x > 88.72283935546875f)
-        return INFINITY;
-    if (x < -103.972084045410156f)
-        return 0.0f;
-    const float kf = rintf(x * 1.44269502162933349609f);
-    const float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187045e-06f;
-    float p = 1.0f / 5040.0f;
-    p = p * r + 1.0f / 720.0f;
-    p = p * r + 1.0f / 120.0f;
-    p = p * r + 1.0f / 24.0f;
-    p = p * r + 1.0f / 6.0f;
-    p = p * r + 0.5f;
-    p = p * r + 1.0f;
-    p = p * r + 1.0f;
-    int k = (int)kf;
-    int k1 = k / 2, k2 = k - k / 2;
-    union { uint32_t u; float f; } a, b;
-    a.u = (uint32_t)(k1 + 127) << 23;
-    b.u = (uint32_t)(k2 + 127) << 23;
-    return (p * a.f) * b.f;
-}
+/* exp(x) as the frame kernel evaluates it (det_expf.h: Cody-Waite reduction and a
+ * degree-7 Taylor polynomial, at most 2 ulp from exp(x)) */
+static inline float orc_expf(float x) { return gca_det_expf(x); }
 
 float orc_exp32(float x) { return orc_expf(x); }
 

@@ -50,6 +50,50 @@ class Golden(dict):
     def gn_src_rgb(self):
         return self["cloud_rgb"][8000:12000]
 
+    # --- the RGB-D frame fixture (the reference's cuda_point_cloud_factory.cu helpers) ---
+    FRAME_CASES = ("raw", "adaptive", "fixed", "adaptive_extrinsic", "adaptive_tmin0")
+    FRAME_FIXED = (2, 3.0, 30.0)  # radius, sigma_space (px), sigma_depth (depth units)
+
+    def frame_case(self, name):
+        """(depth intrinsics, colour intrinsics, rotation (9, column-major), translation,
+        filter mode, tmin) of a frame case"""
+        a = self[f"frame_{name}_args"]
+        return (tuple(map(float, a[0:4])), tuple(map(float, a[4:8])), a[8:17].copy(), a[17:20].copy(), int(a[20]),
+                float(a[21]))
+
+    def check_frame(self, name, xyz, rgb, depth=None):
+        """Against the frame helpers built with the Cody-Waite exp of the frame kernel:
+        bit for bit.  Against the helpers with the host's expf: the filtered depth and
+        the points within 8 ulp (the two exps differ by up to about 2 ulp per weight),
+        the same points in the same raster order, and the same colours except where the
+        colour-image coordinate + 0.5 lies within 1e-4 of an integer, where an ulp of
+        depth moves the colour lookup to the next pixel (at most 3 % of the points)."""
+        k = f"frame_{name}"
+        np.testing.assert_array_equal(xyz, self[k + "_detexp_xyz"])
+        np.testing.assert_array_equal(rgb, self[k + "_detexp_rgb"])
+        if depth is not None:
+            np.testing.assert_array_equal(depth, self[k + "_detexp_depth"])
+        if k + "_stock_xyz" not in self:
+            return
+        sx, sc, scuv = self[k + "_stock_xyz"], self[k + "_stock_rgb"], self[k + "_stock_cuv"]
+        assert len(xyz) == len(sx)
+
+        def ulp(a, b):
+            nan = np.isnan(a) | np.isnan(b)
+            assert (np.isnan(a) == np.isnan(b)).all()
+            d = np.abs(a.view(np.int32).astype(np.int64) - b.view(np.int32).astype(np.int64))
+            return np.where(nan, 0, d).max() if d.size else 0
+
+        assert ulp(xyz, sx) <= 8
+        if depth is not None:
+            assert ulp(depth, self[k + "_stock_depth"]) <= 8
+        differ = (rgb != sc).any(1)
+        finite = np.isfinite(scuv).all(1)
+        edge = np.zeros(len(scuv), bool)
+        edge[finite] = (np.abs(scuv[finite] - np.round(scuv[finite])) < 1e-4).any(1)
+        assert not (differ & ~edge).any()
+        assert differ.sum() <= 0.03 * len(rgb)
+
 
 @pytest.fixture(scope="session")
 def golden():

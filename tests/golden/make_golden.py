@@ -27,10 +27,39 @@ from cuda_3d_gb300 import synth  # noqa: E402
 OUT = os.path.join(HERE, "golden.npz")
 
 
+REF_SRC = os.environ.get("GCA_REF_SRC", "/root/reference/src")
+
+# the frame fixture: a small RGB-D frame of the frame scene, and the cases run through
+# the reference's frame helpers (oracle/ref_frame.inc): (name, filter mode, tmin,
+# depth-to-colour rotation (column-major, as gca::extrinsics stores it), translation,
+# colour intrinsics or None for the depth intrinsics)
+FRAME_CAM = synth.Camera(96, 72, 78.75, 78.75, 47.5, 35.5)
+FRAME_CASES = [
+    ("raw", 0, 0.2, None, None, None),
+    ("adaptive", 1, 0.2, None, None, None),
+    ("fixed", 2, 0.2, None, None, None),
+    ("adaptive_extrinsic", 1, 0.2, "rot", (0.025, -0.01, 0.004), (78.0, 80.5, 48.1, 34.8)),
+    ("adaptive_tmin0", 1, 0.0, None, None, None),
+]
+FRAME_FIXED = (2, 3.0, 30.0)  # radius, sigma_space (px), sigma_depth (depth units)
+# frame_<case>_args: depth intrinsics (4), colour intrinsics (4), rotation (9), translation (3), mode, tmin
+
+
+def frame_case_args(case):
+    name, mode, tmin, rot, tr, ci = case
+    di = np.array([FRAME_CAM.fx, FRAME_CAM.fy, FRAME_CAM.cx, FRAME_CAM.cy], np.float32)
+    R = np.eye(3, dtype=np.float32)
+    if rot == "rot":
+        R = f32(synth.axis_angle([0.2, 1.0, -0.3], np.radians(1.0)))
+    return (di, np.array(ci, np.float32) if ci else di, f32(R.T.reshape(-1)), f32(tr or (0.0, 0.0, 0.0)), mode,
+            np.float32(tmin))
+
+
 def load_ref(ref_src):
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={ref_src}"], check=True)
     L = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libgca_ref.so"))
-    for f in ("ref_voxel_downsample", "ref_radius_search", "ref_radius_outlier_removal"):
+    for f in ("ref_voxel_downsample", "ref_radius_search", "ref_radius_outlier_removal", "ref_make_point_cloud",
+              "ref_make_point_cloud_detexp"):
         getattr(L, f).restype = C.c_int64
     return L
 
@@ -43,7 +72,7 @@ def f32(a):
     return np.ascontiguousarray(a, np.float32)
 
 
-def main(ref_src="/root/reference/src"):
+def main(ref_src=REF_SRC):
     L = load_ref(ref_src)
     g = {}
     rng = np.random.default_rng(20240601)
@@ -131,6 +160,26 @@ def main(ref_src="/root/reference/src"):
     m = L.ref_radius_outlier_removal(P(pts), P(col), C.c_int64(len(pts)), C.c_float(0.05), 4, P(ro_x), P(ro_c))
     g["ror_radius"], g["ror_min_nn"] = np.float32(0.05), np.int32(4)
     g["ror_xyz"], g["ror_rgb"] = ro_x[:m], ro_c[:m]
+
+    # --- RGB-D frame -> cloud (cuda_point_cloud_factory.cu helpers) ------------
+    depth, bgr = synth.render_rgbd(synth.frame_scene(1234), np.eye(4), 5, FRAME_CAM)[:2]
+    g["frame_depth"], g["frame_bgr"] = depth, bgr
+    n = depth.size
+    for case in FRAME_CASES:
+        di, ci, rot, tr, mode, tmin = frame_case_args(case)
+        runs = (("ref_make_point_cloud_detexp", "detexp"), ("ref_make_point_cloud", "stock"))
+        for fn, tag in runs[:1] if mode == 0 else runs:  # no exp without a filter
+            xyz, rgb = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+            fd, cuv = np.zeros(n, np.float32), np.zeros((n, 2), np.float32)
+            m = getattr(L, fn)(P(depth), P(bgr), C.c_uint32(FRAME_CAM.width), C.c_uint32(FRAME_CAM.height), P(di),
+                               P(ci), P(rot), P(tr), C.c_float(0.001), C.c_float(tmin), C.c_float(10.0), mode,
+                               FRAME_FIXED[0], C.c_float(FRAME_FIXED[1]), C.c_float(FRAME_FIXED[2]), P(xyz), P(rgb),
+                               P(fd), P(cuv))
+            g[f"frame_{case[0]}_args"] = np.concatenate([di, ci, rot, tr, [mode, tmin]]).astype(np.float32)
+            k = f"frame_{case[0]}_{tag}"
+            g[k + "_xyz"], g[k + "_rgb"], g[k + "_depth"] = xyz[:m], rgb[:m], fd.reshape(depth.shape)
+            if tag == "stock":
+                g[k + "_cuv"] = cuv[:m]
 
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT}: {os.path.getsize(OUT) / 1e6:.2f} MB, {len(g)} arrays")

@@ -455,6 +455,29 @@ def test_frame_to_cloud_vs_oracle(ctx, N, orc, frames, mode):
     np.testing.assert_array_equal(d["rgb"], oc)
 
 
+@pytest.mark.parametrize("case", ["raw", "adaptive", "fixed", "adaptive_extrinsic", "adaptive_tmin0"])
+def test_frame_to_cloud_vs_reference_golden(ctx, N, golden, case):
+    """the frame kernel against the reference's own frame helpers
+    (cuda_point_cloud_factory.cu:19-187, host build): bit for bit where those use the
+    kernel's exp, within the stated ulp bounds where they use the host's expf"""
+    di, ci, rot, tr, mode, tmin = golden.frame_case(case)
+    depth, bgr = golden["frame_depth"], golden["frame_bgr"]
+    h, w = depth.shape
+    dbuf, cbuf = ctx.alloc(depth.nbytes), ctx.alloc(bgr.nbytes)
+    dbuf.write(depth)
+    cbuf.write(bgr)
+    out = ctx.cloud(h * w)
+    e = N.Extrinsics()
+    e.rotation[:] = list(map(float, rot))
+    e.translation[:] = list(map(float, tr))
+    r, ss, sd = golden.FRAME_FIXED
+    f = N.Filter(mode, r, ss, sd)
+    ctx.check(ctx.L.gca3d_frame_to_cloud(ctx.h, dbuf.ptr, cbuf.ptr, w, h, C.byref(N.Intrinsics(*di)),
+                                         C.byref(N.Intrinsics(*ci)), C.byref(e), 0.001, tmin, 10.0, C.byref(f), out.h))
+    d = out.download()
+    golden.check_frame(case, d["xyz"], d["rgb"])
+
+
 def test_frame_tmin_zero_nan_quirk(ctx, N, orc, frames):
     """with tmin = 0 the reference turns isolated zero pixels into NaN points
     (0 / 0 in the filter passes both threshold tests); the build keeps that"""

@@ -143,3 +143,16 @@ def test_radius_outlier_removal(golden, orc):
     assert 0 < len(ox) < len(xyz)
     np.testing.assert_array_equal(ox, golden["ror_xyz"])
     np.testing.assert_array_equal(oc, golden["ror_rgb"])
+
+
+@pytest.mark.parametrize("case", ["raw", "adaptive", "fixed", "adaptive_extrinsic", "adaptive_tmin0"])
+def test_frame_stage_vs_reference(orc, golden, case):
+    """bilateral filter (adaptive, fixed, none), back-projection with the half-pixel
+    shift, depth-to-colour extrinsic, colour lookup and raster-order compaction
+    against the reference's own frame helpers (cuda_point_cloud_factory.cu:19-187
+    built as host C++, the kernel body :210-266 restated around them)"""
+    di, ci, rot, tr, mode, tmin = golden.frame_case(case)
+    r, ss, sd = golden.FRAME_FIXED
+    xyz, rgb, fd = orc.make_point_cloud(golden["frame_depth"], golden["frame_bgr"], di, ci, (rot, tr), 0.001, tmin,
+                                        10.0, mode, r, ss, sd, return_depth=True)
+    golden.check_frame(case, xyz, rgb, fd)

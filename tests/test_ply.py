@@ -10,7 +10,9 @@ import os
 import numpy as np
 import pytest
 
-FRAG = "/root/reference/data/frag_115.ply"
+# the reference tree's data/ sits beside its src/ (GCA_REF_SRC)
+FRAG = os.path.join(os.path.dirname(os.environ.get("GCA_REF_SRC", "/root/reference/src").rstrip("/")), "data",
+                    "frag_115.ply")
 
 
 @pytest.fixture(scope="module")
