@@ -66,7 +66,7 @@ def parse_args(argv=None):
     p.add_argument("--no-extras", action="store_true", help="skip the per-row measurements (frame pair, "
                    "single pair, adjoint, stream)")
     p.add_argument("--no-tune", action="store_true", help="default launch shape instead of the autotuner's")
-    p.add_argument("--stream-frames", type=int, default=200, help="frames of the 640x480 stream (720p: half)")
+    p.add_argument("--stream-frames", type=int, default=1000, help="frames of each stream (640x480 and 1280x720)")
     p.add_argument("--frame-pair", type=int, default=0, metavar="PUSHES",
                    help="only the 640x480 frame pair: PUSHES alternating tracker pushes (graph mode, or eager "
                         "with --eager), one JSON line")
@@ -543,8 +543,7 @@ def run_rows(ctx, N, synth, args):
     # C4: tracked stream, 640x480 and 1280x720
     scene = synth.frame_scene(1234)
     for name, cam, nf in (("640x480", synth.Camera(), args.stream_frames),
-                          ("1280x720", synth.Camera(1280, 720, 1050.0, 1050.0, 639.5, 359.5),
-                           max(args.stream_frames // 2, 4))):
+                          ("1280x720", synth.Camera(1280, 720, 1050.0, 1050.0, 639.5, 359.5), args.stream_frames)):
         poses = synth.spline_poses(nf, seed=0)
         frames = [synth.render_rgbd_torch(scene, P, 1000 + k, cam) for k, P in enumerate(poses)]
         row = {"frames": nf}

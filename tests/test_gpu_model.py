@@ -8,6 +8,11 @@ filter) except t_max = 10 m: the synthetic room reaches 4 m, a real camera in th
 was cut at 2.5 m.  Checks:
   * the same loop replayed through the individual stage entry points gives the same
     model, bit for bit, and the same append decisions;
+  * the loop replayed with the FP64 oracle's stages (frame stage, voxels and outlier
+    removal bit-exact, FP64 normals, gradients and colored ICP) gives every
+    registration within 1e-5 rad / 1e-5 m and the same append decisions; the replay
+    moves its model by the GPU's FP32 pose, so both loops hold the same model, which
+    is compared bit for bit at the end;
   * every registration lands near the ground-truth relative motion;
   * the model stays bounded by the re-voxelisation."""
 import ctypes as C
@@ -105,6 +110,60 @@ def test_model_loop_matches_stage_replay(ctx, N, seq):
     np.testing.assert_array_equal(got["rgb"], want["rgb"])
     # bounded by the re-voxelisation: never more than 5 frames' worth above one frame
     assert max(sizes) < 7 * sizes[0]
+
+
+def transform_ref32(T, xyz):
+    """point_cloud::transform (src/geometry/point_cloud.cu:93-105): FP32, unfused
+    ((R0 x + R1 y) + R2 z) + t"""
+    T = np.asarray(T, np.float32)
+    x, y, z = (np.ascontiguousarray(xyz[:, k], np.float32) for k in range(3))
+    return np.stack([((T[r, 0] * x + T[r, 1] * y) + T[r, 2] * z) + T[r, 3] for r in range(3)], 1).astype(np.float32)
+
+
+def test_model_loop_matches_fp64_oracle_replay(ctx, N, orc, seq):
+    """apps/app.cpp:111-128 and 315-349 replayed with the oracle's stages"""
+    from cuda_3d_gb300 import synth
+
+    cam, poses, frames = seq
+    model = N.Model(ctx, N.model_params(cam, tmax=10.0))
+    out = [model.push(d, c) for d, c in frames]
+    got = model.cloud().download(rgb=True)
+    intr = (cam.fx, cam.fy, cam.cx, cam.cy)
+    eps = float(np.float32(1e-6))  # color_icp.hpp:47-48
+    mx = mc = px = pc = None
+    counter = 0
+    for k, (d, c) in enumerate(frames):
+        rx, rc = orc.make_point_cloud(d, c, intr, mode=orc.FILTER_ADAPTIVE, tmin=0.2, tmax=10.0)
+        vx, vc, _, _ = orc.voxel_downsample(rx, rc, 0.008)
+        cx, cc = orc.radius_outlier_removal(vx, vc, 0.01, 4)
+        if k == 0:
+            mx, mc = cx, cc
+        else:
+            sx, sc = (mx, mc) if counter == 0 else (px, pc)
+            tn = orc.normals_f64(cx, 0.04, 0)
+            tg = orc.gradient_f64(cx, cc, tn, 0.05)
+            o = orc.color_icp_f64(sx, sc, cx, cc, tn, tg, max_iter=10, max_corr=0.05, update_map=orc.UPDATE_EULER_ZYX,
+                                  rot_eps=eps, trans_eps=eps)
+            r, appended = out[k]
+            assert r["status"] == N.OK
+            rot, tr = synth.pose_error(r["T"], o.T)
+            assert rot <= 1e-5 and tr <= 1e-5, (k, rot, tr)
+            assert r["iterations"] == o.iterations, k
+            # the append decision of the oracle's own pose (app.cpp:328-340, FP32)
+            Tf = o.T.astype(np.float32)
+            cth = np.float32(0.5) * (Tf[0, 0] + Tf[1, 1] + Tf[2, 2] - np.float32(1))
+            tsq = Tf[0, 3] * Tf[0, 3] + Tf[1, 3] * Tf[1, 3] + Tf[2, 3] * Tf[2, 3]
+            assert appended == bool(cth <= np.float32(0.999999) or tsq >= np.float32(1e-6)), k
+            if appended:
+                mx = np.concatenate([transform_ref32(r["T"].astype(np.float32), mx), cx])
+                mc = np.concatenate([mc, cc])
+                counter += 1
+            if counter == 5:
+                mx, mc, _, _ = orc.voxel_downsample(mx, mc, 0.008)
+                counter = 0
+        px, pc = cx, cc
+    np.testing.assert_array_equal(got["xyz"], mx)
+    np.testing.assert_array_equal(got["rgb"], mc)
 
 
 def test_model_rejects_bad_parameters(ctx, N, seq):

@@ -8,6 +8,9 @@ neighbours, colour gradients with radius 0.02 m, colored ICP with lambda 0.968, 
 most 30 iterations, max correspondence distance 0.03 m.  Checks:
   * every registration equals, bit for bit, the same frames run through the
     individual stage entry points (frame_to_cloud, then color_icp);
+  * every registration is within 1e-5 rad / 1e-5 m of the FP64 oracle run on the
+    oracle's own clouds of the two frames from the same initial pose, with the same
+    iteration count;
   * the captured per-frame graph and the plain eager pipeline give identical poses;
   * the composed trajectory stays within DRIFT_ROT / DRIFT_TRANS of ground truth
     (measured on GB300 after 10 frames: 0.010 rad, 0.017 m; with the reference's
@@ -89,6 +92,29 @@ def test_tracker_matches_stage_entry_points(ctx, N, seq):
         np.testing.assert_array_equal(out[k][0]["T"], r["T"])
         assert out[k][0]["iterations"] == r["iterations"]
         last = r["T"]
+
+
+def test_tracker_matches_fp64_oracle(ctx, N, orc, seq):
+    """per frame: the oracle's frame stage (bit-exact with the kernel's), 0.01 m voxels,
+    FP64 normals (at most 30 neighbours) and gradients, and FP64 colored ICP from the
+    tracker's initial pose for that frame (the previous frame's motion)"""
+    from cuda_3d_gb300 import synth
+
+    cam, poses, frames = seq
+    out, _ = run_tracker(ctx, N, seq, use_graph=True)
+    intr = (cam.fx, cam.fy, cam.cx, cam.cy)
+    clouds = [orc.make_point_cloud(d, c, intr, mode=orc.FILTER_FIXED, radius=2, sigma_space=3.0, sigma_depth=30.0,
+                                   tmin=0.2, tmax=10.0) for d, c in frames]
+    T_init = np.eye(4)
+    for k in range(1, N_FRAMES):
+        (sx, sc), (tx, tc) = clouds[k], clouds[k - 1]
+        T64, res = orc.multiscale_f64(sx, sc, tx, tc, [orc.Scale(0.01, 30, 0.03, 0.02, 0.02, 30)],
+                                      update_map=orc.UPDATE_EULER_ZYX, T_init=T_init)
+        r = out[k][0]
+        rot, tr = synth.pose_error(r["T"], T64)
+        assert rot <= 1e-5 and tr <= 1e-5, (k, rot, tr)
+        assert r["iterations"] == res[0].iterations, k
+        T_init = r["T"]
 
 
 def test_tracker_graph_equals_plain_and_follows_ground_truth(ctx, N, seq):
