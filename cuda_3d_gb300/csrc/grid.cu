@@ -77,11 +77,14 @@ __global__ void k_grid_layout(const int *ord, int P, float cell, int mode, float
 }
 
 __global__ void k_grid_keys(const float4 *__restrict__ pos, const int32_t *seg_off, const float3 *origin,
-                            const KeyLayout *lay, float cell, uint64_t *keys, int32_t *vals)
+                            const KeyLayout *lay, float cell, uint64_t *keys, int32_t *vals, int ib_cap, int *d_ib)
 {
     const int seg = blockIdx.y;
     const int b = seg_off[seg], e = seg_off[seg + 1];
     const KeyLayout L = *lay;
+    const int ib = packed_index_bits(L.total_bits, ib_cap);
+    if (seg == 0 && blockIdx.x == 0 && threadIdx.x == 0)
+        *d_ib = ib;
     const float3 o = origin[seg];
     const uint64_t mask_x = (1ull << L.bx) - 1, mask_y = (1ull << L.by) - 1, mask_z = (1ull << L.bz) - 1;
     for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x)
@@ -91,8 +94,8 @@ __global__ void k_grid_keys(const float4 *__restrict__ pos, const int32_t *seg_o
         uint64_t cx = (uint64_t)max(cell_of(p.x, o.x, cell), 0) & mask_x;
         uint64_t cy = (uint64_t)max(cell_of(p.y, o.y, cell), 0) & mask_y;
         uint64_t cz = (uint64_t)max(cell_of(p.z, o.z, cell), 0) & mask_z;
-        keys[i] = ((uint64_t)seg << (L.bx + L.by + L.bz)) | (cx << (L.by + L.bz)) | (cy << L.bz) | cz;
-        vals[i] = i;
+        sort_store(keys, vals, i, ((uint64_t)seg << (L.bx + L.by + L.bz)) | (cx << (L.by + L.bz)) | (cy << L.bz) | cz,
+                   ib);
     }
 }
 
@@ -100,14 +103,13 @@ __global__ void k_grid_scatter(SortBuffers sb, const int32_t *d_n, const KeyLayo
                                float4 *spos, int32_t *sidx, float *sint, int *scz, uint64_t *skey, int *err)
 {
     const int n = *d_n;
-    const uint64_t *keys = sb.keys[*sb.d_sel];
-    const int32_t *vals = sb.vals[*sb.d_sel];
+    const SortedView sv = sorted_view(sb);
     const KeyLayout L = *lay;
     const uint64_t mz = (1ull << L.bz) - 1;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
     {
-        uint64_t k = keys[s];
-        int g = vals[s];
+        uint64_t k = sv.key(s);
+        int g = sv.val(s);
         if (!GCA_INDEX_OK(g, n, err))
             continue;
         float4 p = pos[g];
@@ -205,8 +207,9 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     sb.vals[0] = A.get<int32_t>(cap);
     sb.vals[1] = A.get<int32_t>(cap);
     sb.d_sel = A.get<int>(1);
+    sb.d_ib = A.get<int>(1);
     if (!d.gmin || !d.layout || !d.spos || !d.sidx || !d.sint || !d.scz || !d.skey || !d.slots || !ord || !sb.keys[1] ||
-        !sb.vals[1] || !sb.d_sel)
+        !sb.vals[1] || !sb.d_sel || !sb.d_ib)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "grid_build: scratch");
     cudaStream_t s = ctx->stream;
     int st = seg_bounds(ctx, b.pos, b.seg_off, P, b.max_seg_cap, ord);
@@ -216,10 +219,11 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     k_grid_layout<<<1, 256, 0, s>>>(ord, P, cell, origin_mode, given, d.gmin, d.layout, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     const int gx = std::min(grid_for(b.max_seg_cap, kBlock * 4), ctx->num_sms * 4);
-    k_grid_keys<<<dim3(gx, P), kBlock, 0, s>>>(b.pos, b.seg_off, d.gmin, d.layout, cell, sb.keys[0], sb.vals[0]);
+    k_grid_keys<<<dim3(gx, P), kBlock, 0, s>>>(b.pos, b.seg_off, d.gmin, d.layout, cell, sb.keys[0], sb.vals[0],
+                                               index_bits(cap), sb.d_ib);
     GCA_CHECK_LAUNCH(ctx);
     const int32_t *d_n = b.seg_off + P;
-    st = radix_sort(ctx, sb, d_n, cap, 64, nullptr);
+    st = radix_sort(ctx, sb, b.seg_off, P, cap, b.max_seg_cap, 64);
     if (st)
         return st;
     const int gs = std::min(grid_for(cap), ctx->num_sms * 8);

@@ -366,14 +366,68 @@ static __device__ __noinline__ int2 row_probe_rest(const RowSlot *slots, uint32_
 // radix sort of (key, value) pairs by the low `max_bits` bits, n on the device.
 // keys/vals are ping-pong buffers of capacity `cap`; on return *result_in_alt
 // (device int) says whether the sorted data is in the alternate buffers.
+// A sort of (key, index) pairs runs in one of two forms, chosen on the device by the
+// kernel that writes the keys, once the key layout is known: packed, (key << ib) |
+// index in one 64-bit word, when the key's bits and ib (the bits of the largest index)
+// fit in 64 -- 8 bytes per element each way per pass instead of 12 -- or keys and
+// indices in separate arrays.  The index is the element's position when the keys are
+// written, so in both forms equal keys keep ascending index order.
 struct SortBuffers
 {
     uint64_t *keys[2];
     int32_t *vals[2];
     int *d_sel; // device: index of the buffer holding the sorted data
+    int *d_ib;  // device: index bits of the packed form, 0 for separate arrays
 };
-int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t cap, int max_bits,
-               const int *d_key_bits /* device: bits actually used, or nullptr */);
+
+// index bits of a sort of at most cap elements
+inline int index_bits(int64_t cap)
+{
+    int b = 1;
+    while ((1ll << b) < cap)
+        ++b;
+    return b;
+}
+
+// the packed form's index bits for a key of key_bits bits, or 0 when it does not fit
+__device__ __forceinline__ int packed_index_bits(int key_bits, int ib) { return key_bits + ib <= 64 ? ib : 0; }
+
+// element i of the key kernels' output: key and index i
+__device__ __forceinline__ void sort_store(uint64_t *keys, int32_t *vals, int i, uint64_t key, int ib)
+{
+    if (ib)
+        keys[i] = (key << ib) | (uint64_t)(uint32_t)i;
+    else
+    {
+        keys[i] = key;
+        vals[i] = i;
+    }
+}
+
+// the sorted keys and indices, whichever the form
+struct SortedView
+{
+    const uint64_t *k;
+    const int32_t *v;
+    int ib;
+    __device__ __forceinline__ uint64_t key(int i) const { return ib ? k[i] >> ib : k[i]; }
+    __device__ __forceinline__ int32_t val(int i) const
+    {
+        return ib ? (int32_t)(k[i] & ((1ull << ib) - 1ull)) : v[i];
+    }
+};
+__device__ __forceinline__ SortedView sorted_view(const SortBuffers &sb)
+{
+    const int sel = *sb.d_sel;
+    return SortedView{sb.keys[sel], sb.vals[sel], *sb.d_ib};
+}
+
+// stable LSD sort of the keys in sb.keys[0] (and sb.vals[0]) in place, segment by
+// segment: seg_off[P + 1] (device) holds the segments' element ranges, at most cap
+// elements in all and max_seg_cap in one segment; the segment index must be the keys'
+// most significant field
+int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *seg_off, int P, int64_t cap, int64_t max_seg_cap,
+               int max_bits);
 
 // exclusive scan of int32 values (n on the device), writes total to *d_total
 int exclusive_scan(gca3d_context *ctx, const int32_t *in, int32_t *out, const int32_t *d_n,

@@ -27,13 +27,30 @@ constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kFlagMask = 3u << 30;
 constexpr uint32_t kCountMask = (1u << 30) - 1;
 
+// Control words of one sort.  The keys come in P segments ([seg_off[s], seg_off[s+1]),
+// the segment index being the key's most significant field, each segment's keys in
+// ascending index order), so a segment's keys end up in its own range: the sort runs
+// per segment -- digit offsets per segment, tiles that never straddle two segments,
+// and a look-back that ends at the segment's first tile, so the look-back chains are
+// as long as a segment, not as the batch.  A pass is skipped when every segment's
+// keys share its digit (the segment field's digits always do).
 struct SortCtl
 {
-    uint32_t hist[8][256];
-    uint32_t off[8][256];
-    int trivial[8];
+    int nontrivial[8];
     int in_sel[8];
     uint32_t tile_ctr[8];
+    uint32_t prep_ticket;
+    int ntiles; // tiles over all segments
+};
+
+// per-segment scratch of a sort: hist[s][d][b] digit counts, doff[s][d][b] the first
+// output position of bucket b of digit d in segment s, tile_first[s] the segment's
+// first tile (P + 1 entries)
+struct SortSeg
+{
+    uint32_t *hist;
+    uint32_t *doff;
+    int32_t *tile_first;
 };
 
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v)
@@ -65,40 +82,56 @@ __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long l
     return v;
 }
 
-// histogram of all 8 byte-digits; also clears the first look-back status buffer
-__global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *d_n, SortCtl *ctl,
+// the byte-digit d of a sort word: bits [ib + 8 d, ib + 8 d + 8) (ib = 0 for separate
+// keys and indices), zero above bit 63
+__device__ __forceinline__ uint32_t sort_digit(uint64_t k, int ib, int d)
+{
+    const int sh = ib + 8 * d;
+    return sh < 64 ? (uint32_t)(k >> sh) & 255u : 0u;
+}
+
+// per-segment histograms of all 8 byte-digits (block (x, s): segment s); also clears
+// the first look-back status buffer
+__global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *seg_off, const int *d_ib, SortSeg S,
                             uint32_t *status0, int64_t status_words)
 {
     __shared__ uint32_t h[8][256];
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
         (&h[0][0])[i] = 0;
     __syncthreads();
-    const int n = *d_n;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    const int seg = blockIdx.y;
+    const int b = seg_off[seg], e = seg_off[seg + 1];
+    const int ib = *d_ib;
+    for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x)
     {
         uint64_t k = keys[i];
 #pragma unroll
         for (int d = 0; d < 8; ++d)
-            atomicAdd(&h[d][(k >> (8 * d)) & 255], 1u);
+            atomicAdd(&h[d][sort_digit(k, ib, d)], 1u);
     }
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < status_words;
-         i += (int64_t)gridDim.x * blockDim.x)
+    const int64_t nb = (int64_t)gridDim.x * gridDim.y, bid = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+    for (int64_t i = bid * blockDim.x + threadIdx.x; i < status_words; i += nb * blockDim.x)
         status0[i] = 0;
     __syncthreads();
+    uint32_t *gh = S.hist + (size_t)seg * 8 * 256;
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x)
     {
         uint32_t c = (&h[0][0])[i];
         if (c)
-            atomicAdd(&(&ctl->hist[0][0])[i], c);
+            atomicAdd(&gh[i], c);
     }
 }
 
-// bucket offsets per digit, trivial-pass detection and ping-pong bookkeeping: one
-// warp per digit, each lane scanning 8 consecutive buckets
-__global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *d_sel)
+// per segment (block s): bucket offsets of every digit, whether the segment's digit
+// varies, and its tile count; the last block: the segments' first tiles and the
+// ping-pong bookkeeping.  One warp per digit, each lane scanning 8 consecutive buckets.
+__global__ void k_sort_prep(SortCtl *ctl, SortSeg S, const int32_t *seg_off, int P, int npasses, int *d_sel)
 {
-    const int n = *d_n;
+    const int seg = blockIdx.x;
+    const int b = seg_off[seg], n = seg_off[seg + 1] - b;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t *gh = S.hist + (size_t)seg * 8 * 256;
+    uint32_t *go = S.doff + (size_t)seg * 8 * 256;
     for (int d = warp; d < npasses; d += blockDim.x >> 5)
     {
         uint32_t c[8], sum = 0;
@@ -106,7 +139,7 @@ __global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *
 #pragma unroll
         for (int k = 0; k < 8; ++k)
         {
-            c[k] = ctl->hist[d][8 * lane + k];
+            c[k] = gh[d * 256 + 8 * lane + k];
             sum += c[k];
             triv |= (int)c[k] == n;
         }
@@ -118,25 +151,88 @@ __global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *
             if (lane >= o)
                 incl += y;
         }
-        uint32_t run = incl - sum;
+        uint32_t run = (uint32_t)b + incl - sum;
 #pragma unroll
         for (int k = 0; k < 8; ++k)
         {
-            ctl->off[d][8 * lane + k] = run;
+            go[d * 256 + 8 * lane + k] = run;
             run += c[k];
         }
         triv = __any_sync(0xffffffffu, triv);
-        if (lane == 0)
-            ctl->trivial[d] = triv;
+        if (lane == 0 && !triv)
+            atomicOr(&ctl->nontrivial[d], 1);
+    }
+    if (threadIdx.x == 0)
+        S.tile_first[seg + 1] = (n + kSortTile - 1) / kSortTile;
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0)
+        s_last = atomicAdd(&ctl->prep_ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last)
+        return;
+    __threadfence();
+    // exclusive prefix of the tile counts (P <= 4096: 16 per thread, then a block scan)
+    __shared__ int s_part[256];
+    constexpr int kPer = (kMaxSegments + 255) / 256;
+    const int p0 = threadIdx.x * kPer;
+    int cnt[kPer], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+    {
+        cnt[k] = p0 + k < P ? __ldcg(&S.tile_first[p0 + k + 1]) : 0;
+        sum += cnt[k];
+    }
+    s_part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x < 32)
+    {
+        int v[8], t = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            v[k] = s_part[threadIdx.x * 8 + k];
+            t += v[k];
+        }
+        int incl = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)threadIdx.x >= o)
+                incl += y;
+        }
+        int run = incl - t;
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            s_part[threadIdx.x * 8 + k] = run;
+            run += v[k];
+        }
     }
     __syncthreads();
+    int run = s_part[threadIdx.x];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k)
+        if (p0 + k < P)
+        {
+            S.tile_first[p0 + k] = run;
+            run += cnt[k];
+        }
+    if (threadIdx.x == 255)
+    {
+        // the last thread's running sum is the total
+        ctl->ntiles = run;
+        S.tile_first[P] = run;
+    }
     if (threadIdx.x == 0)
     {
         int sel = 0;
         for (int d = 0; d < npasses; ++d)
         {
             ctl->in_sel[d] = sel;
-            if (!ctl->trivial[d])
+            if (__ldcg(&ctl->nontrivial[d]))
                 sel ^= 1;
         }
         *d_sel = sel;
@@ -144,8 +240,9 @@ __global__ void k_sort_prep(SortCtl *ctl, const int32_t *d_n, int npasses, int *
 }
 
 __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
-    uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, uint32_t *status,
-    uint32_t *status_next, int64_t status_words, int pass, const int32_t *d_n, int *d_err)
+    uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, SortSeg S,
+    const int32_t *seg_off, int P, uint32_t *status, uint32_t *status_next, int64_t status_words, int pass,
+    const int *d_ib, int *d_err)
 {
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_excl[256];
@@ -153,28 +250,50 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     __shared__ uint64_t s_keys[kSortTile];
     __shared__ int32_t s_vals[kSortTile];
     __shared__ uint32_t s_tile;
+    __shared__ int s_seg;
     __shared__ uint32_t s_wsum[kSortWarps];
 
     // clear the status buffer of the next pass (the one of the previous pass is done)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < status_words;
          i += (int64_t)gridDim.x * blockDim.x)
         status_next[i] = 0;
-    if (ctl->trivial[pass])
+    if (!ctl->nontrivial[pass])
         return;
-    const int n = *d_n;
-    const int ntiles = (n + kSortTile - 1) / kSortTile;
     if (threadIdx.x == 0)
-        s_tile = atomicAdd(&ctl->tile_ctr[pass], 1u);
+    {
+        const uint32_t tk = atomicAdd(&ctl->tile_ctr[pass], 1u);
+        // the segment of the tile: the last one whose first tile is <= tk (empty
+        // segments share their first tile with the next one)
+        int lo = 0, hi = P - 1;
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.tile_first[mid] <= (int)tk)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        s_tile = tk;
+        s_seg = lo;
+    }
     __syncthreads();
     const uint32_t tile = s_tile;
-    if ((int)tile >= ntiles)
+    if ((int)tile >= ctl->ntiles)
         return;
+    const int seg = s_seg;
+    const int first = S.tile_first[seg];
+    const int seg_b = seg_off[seg], seg_e = seg_off[seg + 1];
+    const int tile_base = seg_b + ((int)tile - first) * kSortTile;
+    const int cnt = min(kSortTile, seg_e - tile_base);
     const int sel = ctl->in_sel[pass];
     const uint64_t *kin = sel ? keys1 : keys0;
     const int32_t *vin = sel ? vals1 : vals0;
     uint64_t *kout = sel ? keys0 : keys1;
     int32_t *vout = sel ? vals0 : vals1;
-    const int shift = pass * 8;
+    // a non-trivial pass lies below bit 64 (the digits above are zero, so trivial)
+    const int ib = *d_ib;
+    const bool packed = ib != 0;
+    const int shift = ib + pass * 8;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
 
@@ -185,15 +304,15 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     uint64_t k[kSortItems];
     int32_t v[kSortItems];
     uint32_t dig[kSortItems], rank[kSortItems];
-    const int64_t base = (int64_t)tile * kSortTile + warp * 32 * kSortItems;
+    const int base = warp * 32 * kSortItems; // within the tile
 #pragma unroll
     for (int it = 0; it < kSortItems; ++it)
     {
-        int64_t idx = base + it * 32 + lane;
-        if (idx < n)
+        const int idx = base + it * 32 + lane;
+        if (idx < cnt)
         {
-            k[it] = kin[idx];
-            v[it] = vin[idx];
+            k[it] = kin[tile_base + idx];
+            v[it] = packed ? 0 : vin[tile_base + idx];
             dig[it] = (uint32_t)(k[it] >> shift) & 255u;
         }
         else
@@ -230,9 +349,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
         s_whist[w][t] = tot;
         tot += c;
     }
-    // this tile's count of digit t, published for the tiles after it
+    // this tile's count of digit t, published for the segment's tiles after it
     uint32_t *st = status + (int64_t)tile * 256 + t;
-    st_release(st, (tile == 0 ? kFlagInc : kFlagAgg) | tot);
+    st_release(st, (tile == first ? kFlagInc : kFlagAgg) | tot);
     // exclusive scan of the tile totals over digits (block scan of 256 values)
     uint32_t x = tot;
 #pragma unroll
@@ -256,28 +375,30 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
 #pragma unroll
     for (int it = 0; it < kSortItems; ++it)
     {
-        if (base + it * 32 + lane < n)
+        if (base + it * 32 + lane < cnt)
         {
             const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
             const uint32_t pl = s_excl[d] + s_whist[warp][d] + rank[it];
             s_keys[pl] = k[it];
-            s_vals[pl] = v[it];
+            if (!packed)
+                s_vals[pl] = v[it];
         }
     }
-    // decoupled look-back across tiles for digit t
+    // decoupled look-back across the segment's earlier tiles for digit t
     uint32_t excl = 0;
-    if (tile > 0)
+    if ((int)tile > first)
     {
         // the predecessors' states for this digit, kLookWindow at a time (independent
-        // relaxed loads), consumed nearest first up to the nearest inclusive one
+        // relaxed loads), consumed nearest first up to the nearest inclusive one (the
+        // segment's first tile publishes an inclusive state at once)
         bool found = false;
         const uint32_t limit = wait_limit(d_err);
-        for (int64_t p = (int64_t)tile - 1; p >= 0 && !found; p -= kLookWindow)
+        for (int64_t p = (int64_t)tile - 1; p >= first && !found; p -= kLookWindow)
         {
             uint32_t s[kLookWindow];
 #pragma unroll
             for (int j = 0; j < kLookWindow; ++j)
-                s[j] = p - j >= 0 ? ld_relaxed(status + (p - j) * 256 + t) : kFlagInc;
+                s[j] = p - j >= first ? ld_relaxed(status + (p - j) * 256 + t) : kFlagInc;
 #pragma unroll
             for (int j = 0; j < kLookWindow; ++j)
             {
@@ -302,48 +423,57 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
         }
         st_release(st, kFlagInc | (excl + tot));
     }
-    s_gbase[t] = ctl->off[pass][t] + excl - tile_excl;
+    s_gbase[t] = S.doff[((size_t)seg * 8 + pass) * 256 + t] + excl - tile_excl;
     __syncthreads();
-    const int cnt = min(kSortTile, n - (int)tile * kSortTile);
     for (int j = threadIdx.x; j < cnt; j += kSortThreads)
     {
         uint64_t kk = s_keys[j];
         uint32_t d = (uint32_t)(kk >> shift) & 255u;
         uint32_t g = s_gbase[d] + j;
-        if (!GCA_INDEX_OK(g, n, d_err))
+        if (!GCA_INDEX_OK((int)g - seg_b, seg_e - seg_b, d_err))
             continue;
         kout[g] = kk;
-        vout[g] = s_vals[j];
+        if (!packed)
+            vout[g] = s_vals[j];
     }
 }
 
-int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *d_n, int64_t cap, int max_bits,
-               const int * /*d_key_bits*/)
+int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *seg_off, int P, int64_t cap, int64_t max_seg_cap,
+               int max_bits)
 {
     // four resident tiles per SM (47 KB of shared memory each) need the shared-memory side
     // of the L1 carveout
     static const bool carveout = cudaFuncSetAttribute(k_sort_pass, cudaFuncAttributePreferredSharedMemoryCarveout,
                                                       cudaSharedmemCarveoutMaxShared) == cudaSuccess;
     (void)carveout;
+    if (P < 1 || P > kMaxSegments)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "radix_sort: segment count");
     const int npasses = max_bits <= 0 ? 1 : (max_bits + 7) / 8;
-    const int64_t ntiles = (cap + kSortTile - 1) / kSortTile;
-    const int64_t status_words = (ntiles > 0 ? ntiles : 1) * 256;
+    // tiles never straddle segments: at most one partial tile per segment more
+    const int64_t ntiles = (cap + kSortTile - 1) / kSortTile + P;
+    const int64_t status_words = ntiles * 256;
     SortCtl *ctl = ctx->arena.get<SortCtl>(1);
     uint32_t *status = ctx->arena.get<uint32_t>(2 * status_words);
-    if (!ctl || !status || !sb.d_sel)
+    SortSeg S;
+    S.hist = ctx->arena.get<uint32_t>((size_t)P * 8 * 256);
+    S.doff = ctx->arena.get<uint32_t>((size_t)P * 8 * 256);
+    S.tile_first = ctx->arena.get<int32_t>(P + 1);
+    if (!ctl || !status || !sb.d_sel || !S.hist || !S.doff || !S.tile_first)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "radix_sort: scratch");
     GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(SortCtl), ctx->stream));
-    int hist_grid = (int)std::min<int64_t>(grid_for(cap, kBlock * 8), (int64_t)ctx->num_sms * 8);
-    k_sort_hist<<<hist_grid, kBlock, 0, ctx->stream>>>(sb.keys[0], d_n, ctl, status, status_words);
+    GCA_CUDA(ctx, cudaMemsetAsync(S.hist, 0, sizeof(uint32_t) * (size_t)P * 8 * 256, ctx->stream));
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(grid_for(max_seg_cap, kBlock * 8),
+                                                               ((int64_t)ctx->num_sms * 8 + P - 1) / P));
+    k_sort_hist<<<dim3(gx, P), kBlock, 0, ctx->stream>>>(sb.keys[0], seg_off, sb.d_ib, S, status, status_words);
     GCA_CHECK_LAUNCH(ctx);
-    k_sort_prep<<<1, 256, 0, ctx->stream>>>(ctl, d_n, npasses, sb.d_sel);
+    k_sort_prep<<<P, 256, 0, ctx->stream>>>(ctl, S, seg_off, P, npasses, sb.d_sel);
     GCA_CHECK_LAUNCH(ctx);
     for (int p = 0; p < npasses; ++p)
     {
         GCA_PROF_BEGIN(ctx, kKidSortPass);
-        k_sort_pass<<<(int)(ntiles > 0 ? ntiles : 1), kSortThreads, 0, ctx->stream>>>(
-            sb.keys[0], sb.vals[0], sb.keys[1], sb.vals[1], ctl, status + (p & 1) * status_words,
-            status + ((p + 1) & 1) * status_words, status_words, p, d_n, ctx->d_err);
+        k_sort_pass<<<(int)ntiles, kSortThreads, 0, ctx->stream>>>(
+            sb.keys[0], sb.vals[0], sb.keys[1], sb.vals[1], ctl, S, seg_off, P, status + (p & 1) * status_words,
+            status + ((p + 1) & 1) * status_words, status_words, p, sb.d_ib, ctx->d_err);
         GCA_CHECK_LAUNCH(ctx);
         GCA_PROF_END(ctx, kKidSortPass);
     }

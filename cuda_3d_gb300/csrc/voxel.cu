@@ -163,12 +163,15 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v)
 }
 
 __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3 *origin, const KeyLayout *lay,
-                             float voxel, uint64_t *keys, int32_t *vals)
+                             float voxel, uint64_t *keys, int32_t *vals, int ib_cap, int *d_ib)
 {
     const int seg = blockIdx.y;
     const int n = *src[seg].d_n;
     const int base = off[seg];
     const KeyLayout L = *lay;
+    const int ib = packed_index_bits(L.total_bits, ib_cap);
+    if (seg == 0 && blockIdx.x == 0 && threadIdx.x == 0)
+        *d_ib = ib;
     const float3 o = origin[seg];
     const float4 *pos = src[seg].pos;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -179,17 +182,16 @@ __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3
         const uint64_t key = ((uint64_t)seg << (L.bx + L.by + L.bz)) |
                              (L.morton ? (spread3(kx) << 2) | (spread3(ky) << 1) | spread3(kz)
                                        : (kx << (L.by + L.bz)) | (ky << L.bz) | kz);
-        keys[base + i] = key;
-        vals[base + i] = base + i;
+        sort_store(keys, vals, base + i, key, ib);
     }
 }
 
 __global__ void k_run_flags(SortBuffers sb, const int32_t *d_n, int32_t *flags)
 {
-    const uint64_t *keys = sb.keys[*sb.d_sel];
+    const SortedView sv = sorted_view(sb);
     const int n = *d_n;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        flags[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1 : 0;
+        flags[i] = (i == 0 || sv.key(i) != sv.key(i - 1)) ? 1 : 0;
 }
 
 // run starts of the sorted keys, and the first run (voxel) of every segment
@@ -197,7 +199,7 @@ __global__ void k_run_starts(const int32_t *flags, const int32_t *vid, const int
                              int32_t *starts, SortBuffers sb, const KeyLayout *lay, int32_t *seg_first)
 {
     const int n = *d_n;
-    const uint64_t *keys = sb.keys[*sb.d_sel];
+    const SortedView sv = sorted_view(sb);
     const KeyLayout L = *lay;
     const int segshift = L.bx + L.by + L.bz;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -205,8 +207,8 @@ __global__ void k_run_starts(const int32_t *flags, const int32_t *vid, const int
         if (!flags[i])
             continue;
         starts[vid[i]] = i;
-        const int seg = L.bseg ? (int)(keys[i] >> segshift) : 0;
-        if (i == 0 || (L.bseg && (int)(keys[i - 1] >> segshift) != seg))
+        const int seg = L.bseg ? (int)(sv.key(i) >> segshift) : 0;
+        if (i == 0 || (L.bseg && (int)(sv.key(i - 1) >> segshift) != seg))
             seg_first[seg] = vid[i];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -232,25 +234,24 @@ __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuf
                                const int32_t *d_m, const KeyLayout *lay, float4 *opos, float4 *ocol, int *err)
 {
     const int m = *d_m;
-    const uint64_t *keys = sb.keys[*sb.d_sel];
-    const int32_t *vals = sb.vals[*sb.d_sel];
+    const SortedView sv = sorted_view(sb);
     const KeyLayout L = *lay;
     const int segshift = L.bx + L.by + L.bz;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m; v += gridDim.x * blockDim.x)
     {
         const int s = starts[v], e = starts[v + 1];
-        const int seg = L.bseg ? (int)(keys[s] >> segshift) : 0;
+        const int seg = L.bseg ? (int)(sv.key(s) >> segshift) : 0;
         const int base = in_off[seg];
         const float4 *ps = src[seg].pos;
         const float4 *cs = src[seg].col;
-        int g = vals[s] - base;
+        int g = sv.val(s) - base;
         if (!GCA_INDEX_OK(g, in_off[seg + 1] - base, err))
             continue;
         float4 p = ps[g], c = cs[g];
         float sx = p.x, sy = p.y, sz = p.z, cr = c.x, cg = c.y, cb = c.z;
         for (int j = s + 1; j < e; ++j)
         {
-            g = vals[j] - base;
+            g = sv.val(j) - base;
             if (!GCA_INDEX_OK(g, in_off[seg + 1] - base, err))
                 break;
             p = ps[g];
@@ -287,12 +288,13 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     sb.vals[0] = A.get<int32_t>(cap);
     sb.vals[1] = A.get<int32_t>(cap);
     sb.d_sel = A.get<int>(1);
+    sb.d_ib = A.get<int>(1);
     int32_t *flags = A.get<int32_t>(cap);
     int32_t *vid = A.get<int32_t>(cap);
     int32_t *starts = A.get<int32_t>(cap + 1);
     int32_t *d_m = A.get<int32_t>(1);
     int32_t *seg_count = A.get<int32_t>(P);
-    if (!in_off || !ord || !origin || !lay || !sb.keys[1] || !sb.vals[1] || !sb.d_sel || !flags ||
+    if (!in_off || !ord || !origin || !lay || !sb.keys[1] || !sb.vals[1] || !sb.d_sel || !sb.d_ib || !flags ||
         !vid || !starts || !d_m || !seg_count)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "voxel_stage: scratch");
     if (!out.pos)
@@ -311,10 +313,11 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     GCA_CHECK_LAUNCH(ctx);
     k_voxel_layout<<<1, 256, 0, s>>>(ord, P, voxel, morton, origin, lay, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
-    k_voxel_keys<<<dim3(gx, P), kBlock, 0, s>>>(d_src, in_off, origin, lay, voxel, sb.keys[0], sb.vals[0]);
+    k_voxel_keys<<<dim3(gx, P), kBlock, 0, s>>>(d_src, in_off, origin, lay, voxel, sb.keys[0], sb.vals[0],
+                                                index_bits(cap), sb.d_ib);
     GCA_CHECK_LAUNCH(ctx);
     const int32_t *d_n = in_off + P;
-    int st = radix_sort(ctx, sb, d_n, total_cap, 64, nullptr);
+    int st = radix_sort(ctx, sb, in_off, P, total_cap, max_seg_cap, 64);
     if (st)
         return st;
     const int gs = std::min(grid_for(total_cap), ctx->num_sms * 8);

@@ -113,6 +113,42 @@ def test_vjp_matches_fp64_adjoint(ctx, N, orc, c2, K, umap):
         assert np.abs(r["dxi0"]).max() <= 1e-3 * np.abs(G).max()
 
 
+@pytest.mark.parametrize("K,rtol", [(2, 2e-3), (3, 1e-2)])
+def test_vjp_pose_gradient_far_from_convergence(ctx, N, orc, c2, K, rtol):
+    """The pose block of the gradient where it is not negligible.  With the
+    correspondences frozen, Gauss-Newton contracts the pose's sensitivity to its start
+    by about 50-100x per step on this pair, so at K = 5 it is below 1e-9 from any
+    start (checked against the oracle); from a start 0.03 rad / 0.03 m off it is 0.04
+    at K = 2 and 2e-4 at K = 3 (|G| = 1.3).  There the GPU's pose gradient must agree
+    with FP64 central differences (h = 1e-4) and the FP64 adjoint within rtol."""
+    umap = 1
+    G, gE = _loss_seed(91)
+    rng = np.random.default_rng(11)
+    xi0 = se3_log(c2["pr"].T_gt) + np.concatenate([rng.normal(size=3) * 0.03, rng.normal(size=3) * 0.03])
+    r = N.color_icp_vjp(ctx, c2["src"], c2["tgt"], xi0, K=K, max_corr=MAX_CORR, update_map=umap, dT=G, dE=gE,
+                        want_corr=True)
+    assert r["status"] == N.OK
+    corr = r["corr"]
+    sx, sc, tx, tc, tn, tg = _oracle_args(c2)
+
+    def L(xi):
+        T, E, _ = orc.icp_unrolled_f64(sx, sc, tx, tc, tn, tg, xi, K=K, max_corr=MAX_CORR, update_map=umap,
+                                       corr=corr)
+        return (G * T).sum() + gE * E
+
+    fd = np.zeros(6)
+    for m in range(6):
+        e = np.zeros(6)
+        e[m] = 1e-4
+        fd[m] = (L(xi0 + e) - L(xi0 - e)) / 2e-4
+    assert np.linalg.norm(fd) > 1e-4 * np.abs(G).max()
+    assert np.linalg.norm(r["dxi0"] - fd) <= rtol * np.linalg.norm(fd), (r["dxi0"], fd)
+    dxi, _, _, st = orc.icp_unrolled_vjp_f64(sx, sc, tx, tc, tn, tg, xi0, corr, G, gE, K=K, max_corr=MAX_CORR,
+                                             update_map=umap)
+    assert st == 0
+    assert np.linalg.norm(r["dxi0"] - dxi) <= rtol * np.linalg.norm(dxi)
+
+
 def test_vjp_matches_finite_differences(ctx, N, orc, c2):
     K, umap = 5, 1
     G, gE = _loss_seed(77)
