@@ -552,8 +552,10 @@ int gca3d_cloud_destroy(gca3d_cloud *c)
 // (page-locked, mapped) host memory or memory of that device; null for anything
 // else -- pageable or managed host memory, another device's memory -- which is
 // copied through a staging buffer instead
-static const float *device_readable(const gca3d_context *ctx, const float *p)
+static const float *device_readable(const gca3d_context *ctx, const float *p, bool *pinned_host = nullptr)
 {
+    if (pinned_host)
+        *pinned_host = false;
     if (!p)
         return nullptr;
     cudaPointerAttributes a{};
@@ -562,9 +564,19 @@ static const float *device_readable(const gca3d_context *ctx, const float *p)
         cudaGetLastError();
         return nullptr;
     }
+    if (pinned_host)
+        *pinned_host = a.type == cudaMemoryTypeHost;
     if (a.type == cudaMemoryTypeHost || (a.type == cudaMemoryTypeDevice && a.device == ctx->device))
         return static_cast<const float *>(a.devicePointer);
     return nullptr;
+}
+
+int gca3d_set_upload_mode(gca3d_context *ctx, int mode)
+{
+    if (!ctx || (mode != GCA3D_UPLOAD_IN_PLACE && mode != GCA3D_UPLOAD_COPY_ENGINE))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "set_upload_mode: unknown mode");
+    ctx->upload_mode = mode;
+    return GCA3D_OK;
 }
 
 int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *c, const float *xyz, const float *rgb, int64_t n)
@@ -612,6 +624,18 @@ int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *c
     UploadBatch B;
     B.count = 0;
     int blocks = 0;
+    // copy-engine mode: pinned sources are first copied into the context scratch
+    const bool staged_mode = ctx->upload_mode == GCA3D_UPLOAD_COPY_ENGINE;
+    if (staged_mode)
+        ctx->arena.reset();
+    auto stage = [&](const float *src, int64_t m, const float **dst) -> int {
+        float *s = ctx->arena.get<float>(3 * std::max<int64_t>(m, 1));
+        if (!s)
+            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "cloud_upload_many: staging");
+        GCA_CUDA(ctx, cudaMemcpyAsync(s, src, sizeof(float) * 3 * m, cudaMemcpyHostToDevice, ctx->stream));
+        *dst = s;
+        return GCA3D_OK;
+    };
     auto flush = [&]() -> int {
         if (B.count == 0)
             return GCA3D_OK;
@@ -625,9 +649,19 @@ int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *c
     {
         gca3d_cloud *c = clouds[k];
         const float *ck = rgb ? rgb[k] : nullptr;
-        const float *dx = n[k] > 0 ? device_readable(ctx, xyz[k]) : nullptr;
-        const float *dc = ck ? device_readable(ctx, ck) : nullptr;
+        bool hx = false, hc = false;
+        const float *dx = n[k] > 0 ? device_readable(ctx, xyz[k], &hx) : nullptr;
+        const float *dc = ck ? device_readable(ctx, ck, &hc) : nullptr;
         int st = GCA3D_OK;
+        if (staged_mode && dx && (!ck || dc))
+        {
+            if (hx)
+                st = stage(xyz[k], n[k], &dx);
+            if (!st && hc)
+                st = stage(ck, n[k], &dc);
+            if (st)
+                return st;
+        }
         // the writes land in call order: queued in-place entries are packed before a
         // staged upload, and before a second entry for a cloud already queued (two
         // entries of one launch would race on the same cloud)

@@ -119,6 +119,7 @@ struct gca3d_context
     // (gca3d_set_wait_limit; kernels read it when they start)
     int *d_err = nullptr;
     int *h_pinned = nullptr; // pinned scratch for small read-backs (64 ints)
+    int upload_mode = 0;     // GCA3D_UPLOAD_IN_PLACE or GCA3D_UPLOAD_COPY_ENGINE
     int64_t launches = 0;
     std::string last_error;
     gca3d::Profiler prof;

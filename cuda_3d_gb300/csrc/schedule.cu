@@ -52,6 +52,10 @@ struct gca3d_icp_plan
     PlanPrologue prologue;       // work enqueued before the schedule (captured with it)
     bool vox_given = false;      // voxel batches supplied by the caller
     PlanVoxels vox;
+    // the initial poses' copy out of h_Tinit, so that an execute that does not wait for
+    // the previous one refills h_Tinit only after that copy has run
+    cudaEvent_t tinit_copied = nullptr;
+    bool tinit_pending = false;
 };
 
 namespace
@@ -295,6 +299,8 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
         cudaStreamSynchronize(pl->ctx->stream);
     if (pl->exec)
         cudaGraphExecDestroy(pl->exec);
+    if (pl->tinit_copied)
+        cudaEventDestroy(pl->tinit_copied);
     if (pl->side)
         cudaStreamDestroy(pl->side);
     if (pl->graph)
@@ -460,11 +466,17 @@ int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_r
     if (!pl)
         return GCA3D_ERR_INVALID_VALUE;
     gca3d_context *ctx = pl->ctx;
+    if (!pl->tinit_copied)
+        GCA_CUDA(ctx, cudaEventCreateWithFlags(&pl->tinit_copied, cudaEventDisableTiming));
+    if (pl->tinit_pending)
+        GCA_CUDA(ctx, cudaEventSynchronize(pl->tinit_copied));
     for (int k = 0; k < pl->P; ++k)
         for (int j = 0; j < 16; ++j)
             pl->h_Tinit[16 * k + j] = T_init ? T_init[16 * k + j] : ((j % 5 == 0) ? 1.0 : 0.0);
     GCA_CUDA(ctx, cudaMemcpyAsync(pl->d_Tinit, pl->h_Tinit, sizeof(double) * 16 * pl->P, cudaMemcpyHostToDevice,
                                   ctx->stream));
+    GCA_CUDA(ctx, cudaEventRecord(pl->tinit_copied, ctx->stream));
+    pl->tinit_pending = true;
     int st;
     if (pl->exec)
     {
@@ -476,6 +488,15 @@ int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_r
         return st;
     if (!results)
         return GCA3D_OK;
+    return gca3d_icp_plan_results(pl, results);
+}
+
+int gca3d_icp_plan_results(gca3d_icp_plan *pl, gca3d_icp_result *results)
+{
+    if (!pl || !results)
+        return GCA3D_ERR_INVALID_VALUE;
+    gca3d_context *ctx = pl->ctx;
+    int st;
     if ((st = read_states(pl)))
         return st;
     if ((st = consume_device_error(ctx, "icp")))

@@ -26,6 +26,7 @@ ERR_CAPACITY = 7
 ERR_NOT_SUPPORTED = 8
 
 FILTER_NONE, FILTER_ADAPTIVE, FILTER_FIXED = 0, 1, 2
+UPLOAD_IN_PLACE, UPLOAD_COPY_ENGINE = 0, 1
 UPDATE_EULER_ZYX, UPDATE_SE3_EXP = 0, 1
 MAX_SCALES = 8
 
@@ -104,6 +105,7 @@ _SIGS = {
     "gca3d_cloud_destroy": [_P],
     "gca3d_cloud_upload": [_P, _P, _P, _P, _I64],
     "gca3d_cloud_upload_many": [_P, C.c_int, _P, _P, _P, _P],
+    "gca3d_set_upload_mode": [_P, C.c_int],
     "gca3d_cloud_set_normals": [_P, _P, _P, _I64],
     "gca3d_cloud_set_gradients": [_P, _P, _P, _I64],
     "gca3d_cloud_capacity": [_P, C.POINTER(_I64)],
@@ -129,6 +131,7 @@ _SIGS = {
     "gca3d_color_icp_batched": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), _P, _P],
     "gca3d_icp_plan_create": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), C.POINTER(_P)],
     "gca3d_icp_plan_execute": [_P, _P, _P],
+    "gca3d_icp_plan_results": [_P, _P],
     "gca3d_icp_plan_destroy": [_P],
     "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
     "gca3d_icp_autotune": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), C.c_int, C.POINTER(Tuning),
@@ -397,6 +400,11 @@ class IcpPlan:
             Ti = np.ascontiguousarray(np.asarray(T_init, np.float64).reshape(self.P, 16))
         self.ctx.check(self.ctx.L.gca3d_icp_plan_execute(self.h, _ptr(Ti), self._res if results else None))
         return [result_dict(r) for r in self._res] if results else None
+
+    def results(self):
+        """the results of the last execute (waits for it)"""
+        self.ctx.check(self.ctx.L.gca3d_icp_plan_results(self.h, self._res))
+        return [result_dict(r) for r in self._res]
 
     def kernels(self):
         n = C.c_int64()

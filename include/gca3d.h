@@ -161,6 +161,16 @@ int gca3d_cloud_upload(gca3d_context *ctx, gca3d_cloud *cloud, const float *xyz,
  * launch per 64; the others go through gca3d_cloud_upload's staging copy. */
 int gca3d_cloud_upload_many(gca3d_context *ctx, int count, gca3d_cloud *const *clouds,
                             const float *const *xyz, const float *const *rgb, const int64_t *n);
+/* how the context's uploads read pinned host memory (no reference counterpart).
+ * GCA3D_UPLOAD_IN_PLACE (default): the packing kernel reads it over the host link
+ * itself -- the fastest upload when nothing else runs.  GCA3D_UPLOAD_COPY_ENGINE: the
+ * GPU's copy engines first copy it into the context's scratch, then the packing kernel
+ * reads that -- the copies occupy no SMs, so the uploads of a context kept for them
+ * overlap the registration running on another context's stream (double buffering).
+ * Device sources are read in place and pageable ones staged in both modes. */
+#define GCA3D_UPLOAD_IN_PLACE 0
+#define GCA3D_UPLOAD_COPY_ENGINE 1
+int gca3d_set_upload_mode(gca3d_context *ctx, int mode);
 /* normals (n x 3) supplied by the caller; marks the cloud as having normals */
 int gca3d_cloud_set_normals(gca3d_context *ctx, gca3d_cloud *cloud, const float *nrm, int64_t n);
 /* colour gradients (n x 3) supplied by the caller; needs normals */
@@ -309,6 +319,10 @@ int gca3d_icp_plan_create(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *s
  * which case execute does not synchronise */
 int gca3d_icp_plan_execute(gca3d_icp_plan *plan, const double *T_init,
                            gca3d_icp_result *results);
+/* the results of the plan's last execute: waits for it on the context stream.  With
+ * execute(..., NULL) first, the host is free in between, e.g. to enqueue the next
+ * step's uploads on another context's stream. */
+int gca3d_icp_plan_results(gca3d_icp_plan *plan, gca3d_icp_result *results);
 int gca3d_icp_plan_destroy(gca3d_icp_plan *plan);
 /* kernels one execute launches (graph nodes, or the eager launches of the last run) */
 int gca3d_icp_plan_kernels(gca3d_icp_plan *plan, int64_t *n);

@@ -82,10 +82,12 @@ def test_upload_from_pinned_and_device_memory(ctx, N, golden):
         np.testing.assert_array_equal(got[1], want[1])
 
 
-def test_upload_many_matches_single_uploads(ctx, N, golden):
+@pytest.mark.parametrize("mode", ["in_place", "copy_engine"])
+def test_upload_many_matches_single_uploads(ctx, N, golden, mode):
     """One batched call over clouds of mixed sources (pinned, device, pageable, no
-    colour, empty) gives the clouds of the single uploads."""
+    colour, empty) gives the clouds of the single uploads, in both upload modes."""
     torch = pytest.importorskip("torch")
+    ctx.check(ctx.L.gca3d_set_upload_mode(ctx.h, N.UPLOAD_COPY_ENGINE if mode == "copy_engine" else N.UPLOAD_IN_PLACE))
     xyz, rgb = golden["cloud_xyz"], golden["cloud_rgb"]
     n = len(xyz)
     parts = [(0, n), (0, 1000), (5, 4000), (100, 100), (7, n)]
@@ -106,11 +108,13 @@ def test_upload_many_matches_single_uploads(ctx, N, golden):
         ref = ctx.cloud_from(xyz[a:b], rgb[a:b] if with_rgb else None, capacity=max(b - a, 1))
         want.append(ref.download())
     N.upload_many(ctx, clouds, xp, rp, cnt)
+    ctx.check(ctx.L.gca3d_set_upload_mode(ctx.h, N.UPLOAD_IN_PLACE))
     for c, w, m in zip(clouds, want, cnt):
         assert len(c) == m
         d = c.download()
         np.testing.assert_array_equal(d["xyz"], w["xyz"])
         np.testing.assert_array_equal(d["rgb"], w["rgb"])
+    assert ctx.L.gca3d_set_upload_mode(ctx.h, 7) == N.ERR_INVALID_VALUE
 
 
 def test_upload_many_repeated_cloud_keeps_call_order(ctx, N, golden):
