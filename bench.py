@@ -67,6 +67,9 @@ def parse_args(argv=None):
                    "single pair, adjoint, stream)")
     p.add_argument("--no-tune", action="store_true", help="default launch shape instead of the autotuner's")
     p.add_argument("--stream-frames", type=int, default=1000, help="frames of each stream (640x480 and 1280x720)")
+    p.add_argument("--single-pair", type=int, default=0, metavar="EXECUTES",
+                   help="only the 250k-point pair through three scales: EXECUTES plan executes (graph mode, or "
+                        "eager with --eager), one JSON line")
     p.add_argument("--frame-pair", type=int, default=0, metavar="PUSHES",
                    help="only the 640x480 frame pair: PUSHES alternating tracker pushes (graph mode, or eager "
                         "with --eager), one JSON line")
@@ -683,10 +686,35 @@ def run_frame_pair(args):
                       **_lat(steady), "iterations": res[-1]["iterations"], "kernels_per_push": kern}))
 
 
+def run_single_pair(args):
+    """the 250k-point pair through three scales alone (the per-row measurement of
+    run_rows), e.g. under a profiler"""
+    from cuda_3d_gb300 import build, native as N
+    from cuda_3d_gb300 import synth
+
+    build.build()
+    ctx = N.Context(0)
+    pr = synth.room_pair(seed=1, n_points=250_000, rot_deg=10.0, trans=0.10)
+    s = ctx.cloud_from(pr.src_xyz, pr.src_rgb)
+    t = ctx.cloud_from(pr.tgt_xyz, pr.tgt_rgb)
+    plan = N.IcpPlan(ctx, [s], [t], N.icp_params([N.scale(*x) for x in SCALES], update_map=N.UPDATE_SE3_EXP,
+                                                 compensated=True, use_graph=not args.eager))
+    ms = []
+    for _ in range(args.single_pair):
+        t0 = time.perf_counter()
+        r = plan.execute(results=True)[0]
+        ms.append((time.perf_counter() - t0) * 1e3)
+    steady = ms[2:] if len(ms) > 4 else ms[1:] or ms
+    print(json.dumps({"metric": "250k-point pair, three scales (ms per execute, resident clouds)",
+                      "executes": len(ms), **_lat(steady), "iterations": r["iterations"]}))
+
+
 def main(argv=None):
     args = parse_args(argv)
     if args.impl == "reference":
         run_reference(args)
+    elif args.single_pair:
+        run_single_pair(args)
     elif args.frame_pair:
         run_frame_pair(args)
     else:

@@ -77,14 +77,15 @@ __global__ void k_grid_layout(const int *ord, int P, float cell, int mode, float
 }
 
 __global__ void k_grid_keys(const float4 *__restrict__ pos, const int32_t *seg_off, const float3 *origin,
-                            const KeyLayout *lay, float cell, uint64_t *keys, int32_t *vals, int ib_cap, int *d_ib)
+                            const KeyLayout *lay, float cell, uint64_t *keys, int32_t *vals, int ib_cap, int *d_ib,
+                            int *d_kshift)
 {
     const int seg = blockIdx.y;
     const int b = seg_off[seg], e = seg_off[seg + 1];
     const KeyLayout L = *lay;
     const int ib = packed_index_bits(L.total_bits, ib_cap);
     if (seg == 0 && blockIdx.x == 0 && threadIdx.x == 0)
-        *d_ib = ib;
+        *d_ib = *d_kshift = ib;
     const float3 o = origin[seg];
     const uint64_t mask_x = (1ull << L.bx) - 1, mask_y = (1ull << L.by) - 1, mask_z = (1ull << L.bz) - 1;
     for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x)
@@ -208,8 +209,9 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     sb.vals[1] = A.get<int32_t>(cap);
     sb.d_sel = A.get<int>(1);
     sb.d_ib = A.get<int>(1);
+    sb.d_kshift = A.get<int>(1);
     if (!d.gmin || !d.layout || !d.spos || !d.sidx || !d.sint || !d.scz || !d.skey || !d.slots || !ord || !sb.keys[1] ||
-        !sb.vals[1] || !sb.d_sel || !sb.d_ib)
+        !sb.vals[1] || !sb.d_sel || !sb.d_ib || !sb.d_kshift)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "grid_build: scratch");
     cudaStream_t s = ctx->stream;
     int st = seg_bounds(ctx, b.pos, b.seg_off, P, b.max_seg_cap, ord);
@@ -220,7 +222,7 @@ int grid_build(gca3d_context *ctx, const Batch &b, float cell, int origin_mode, 
     GCA_CHECK_LAUNCH(ctx);
     const int gx = std::min(grid_for(b.max_seg_cap, kBlock * 4), ctx->num_sms * 4);
     k_grid_keys<<<dim3(gx, P), kBlock, 0, s>>>(b.pos, b.seg_off, d.gmin, d.layout, cell, sb.keys[0], sb.vals[0],
-                                               index_bits(cap), sb.d_ib);
+                                               index_bits(cap), sb.d_ib, sb.d_kshift);
     GCA_CHECK_LAUNCH(ctx);
     const int32_t *d_n = b.seg_off + P;
     st = radix_sort(ctx, sb, b.seg_off, P, cap, b.max_seg_cap, 64);

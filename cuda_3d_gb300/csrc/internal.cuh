@@ -377,8 +377,10 @@ struct SortBuffers
 {
     uint64_t *keys[2];
     int32_t *vals[2];
-    int *d_sel; // device: index of the buffer holding the sorted data
-    int *d_ib;  // device: index bits of the packed form, 0 for separate arrays
+    int *d_sel;    // device: index of the buffer holding the sorted data
+    int *d_ib;     // device: index bits of the packed form, 0 for separate arrays
+    int *d_kshift; // device: the key's lowest bit in a sort word (ib, plus sub-cell bits a
+                   // voxel stage carries for finer scales); the digits start there
 };
 
 // index bits of a sort of at most cap elements
@@ -393,14 +395,15 @@ inline int index_bits(int64_t cap)
 // the packed form's index bits for a key of key_bits bits, or 0 when it does not fit
 __device__ __forceinline__ int packed_index_bits(int key_bits, int ib) { return key_bits + ib <= 64 ? ib : 0; }
 
-// element i of the key kernels' output: key and index i
-__device__ __forceinline__ void sort_store(uint64_t *keys, int32_t *vals, int i, uint64_t key, int ib)
+// element i of the key kernels' output: the word w (the key, with any sub-cell bits
+// below it) and index i
+__device__ __forceinline__ void sort_store(uint64_t *keys, int32_t *vals, int i, uint64_t w, int ib)
 {
     if (ib)
-        keys[i] = (key << ib) | (uint64_t)(uint32_t)i;
+        keys[i] = (w << ib) | (uint64_t)(uint32_t)i;
     else
     {
-        keys[i] = key;
+        keys[i] = w;
         vals[i] = i;
     }
 }
@@ -410,8 +413,8 @@ struct SortedView
 {
     const uint64_t *k;
     const int32_t *v;
-    int ib;
-    __device__ __forceinline__ uint64_t key(int i) const { return ib ? k[i] >> ib : k[i]; }
+    int ib, kshift;
+    __device__ __forceinline__ uint64_t key(int i) const { return k[i] >> kshift; }
     __device__ __forceinline__ int32_t val(int i) const
     {
         return ib ? (int32_t)(k[i] & ((1ull << ib) - 1ull)) : v[i];
@@ -420,7 +423,7 @@ struct SortedView
 __device__ __forceinline__ SortedView sorted_view(const SortBuffers &sb)
 {
     const int sel = *sb.d_sel;
-    return SortedView{sb.keys[sel], sb.vals[sel], *sb.d_ib};
+    return SortedView{sb.keys[sel], sb.vals[sel], *sb.d_ib, *sb.d_kshift};
 }
 
 // stable LSD sort of the keys in sb.keys[0] (and sb.vals[0]) in place, segment by

@@ -91,6 +91,23 @@ int read_states(gca3d_icp_plan *pl)
     return GCA3D_OK;
 }
 
+// the scales after si whose voxel sizes halve, exactly in float, one after the other:
+// their cells refine scale si's, so one sort at scale si serves them all
+SubLevels finer_scales(const gca3d_icp_params &p, int si)
+{
+    SubLevels sub;
+    float v = p.scales[si].voxel;
+    for (int k = si + 1; k < p.n_scales && sub.n < kMaxSubLevels; ++k)
+    {
+        const float w = p.scales[k].voxel;
+        if (!(w > 0.0f) || w * 2.0f != v)
+            break;
+        sub.voxel[sub.n++] = w;
+        v = w;
+    }
+    return sub;
+}
+
 // enqueue the whole schedule on the context stream (eager or under capture)
 int run_schedule(gca3d_icp_plan *pl, bool capturing)
 {
@@ -100,6 +117,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
     int st = icp_state_init(ctx, pl->d_state, P, pl->d_Tinit);
     if (st)
         return st;
+    VoxelChain chain_src, chain_tgt; // sorted state of the last voxel stage, for finer scales
     for (int si = 0; si < p.n_scales; ++si)
     {
         const gca3d_scale &S = p.scales[si];
@@ -114,10 +132,20 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
                 bs = pl->vox.src[si];
                 bt = pl->vox.tgt[si];
             }
-            if ((st = voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true)))
+            const SubLevels sub = p.tuning.voxel_resort ? SubLevels{} : finer_scales(p, si);
+            const bool refine = chain_src.used < chain_src.levels;
+            st = refine ? voxel_refine(ctx, pl->d_src, chain_src, bs)
+                        : voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true, &sub, &chain_src);
+            if (st)
                 return st;
-            if (!pl->vox_given && (st = voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt, true)))
-                return st;
+            if (!pl->vox_given)
+            {
+                st = chain_tgt.used < chain_tgt.levels
+                         ? voxel_refine(ctx, pl->d_tgt, chain_tgt, bt)
+                         : voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt, true, &sub, &chain_tgt);
+                if (st)
+                    return st;
+            }
         }
         else
         {
@@ -561,7 +589,7 @@ extern "C" int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *
     reps = std::max(reps, 1);
     gca3d_icp_params p = *params;
     const IcpShape s0 = icp_shape(p.tuning);
-    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps};
+    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps, p.tuning.voxel_resort};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     {

@@ -82,17 +82,17 @@ __device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long l
     return v;
 }
 
-// the byte-digit d of a sort word: bits [ib + 8 d, ib + 8 d + 8) (ib = 0 for separate
-// keys and indices), zero above bit 63
-__device__ __forceinline__ uint32_t sort_digit(uint64_t k, int ib, int d)
+// the byte-digit d of a sort word: bits [ks + 8 d, ks + 8 d + 8), ks the key's lowest bit
+// (SortBuffers::d_kshift), zero above bit 63
+__device__ __forceinline__ uint32_t sort_digit(uint64_t k, int ks, int d)
 {
-    const int sh = ib + 8 * d;
+    const int sh = ks + 8 * d;
     return sh < 64 ? (uint32_t)(k >> sh) & 255u : 0u;
 }
 
 // per-segment histograms of all 8 byte-digits (block (x, s): segment s); also clears
 // the first look-back status buffer
-__global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *seg_off, const int *d_ib, SortSeg S,
+__global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *seg_off, const int *d_kshift, SortSeg S,
                             uint32_t *status0, int64_t status_words)
 {
     __shared__ uint32_t h[8][256];
@@ -101,13 +101,13 @@ __global__ void k_sort_hist(const uint64_t *__restrict__ keys, const int32_t *se
     __syncthreads();
     const int seg = blockIdx.y;
     const int b = seg_off[seg], e = seg_off[seg + 1];
-    const int ib = *d_ib;
+    const int ks = *d_kshift;
     for (int i = b + blockIdx.x * blockDim.x + threadIdx.x; i < e; i += gridDim.x * blockDim.x)
     {
         uint64_t k = keys[i];
 #pragma unroll
         for (int d = 0; d < 8; ++d)
-            atomicAdd(&h[d][sort_digit(k, ib, d)], 1u);
+            atomicAdd(&h[d][sort_digit(k, ks, d)], 1u);
     }
     const int64_t nb = (int64_t)gridDim.x * gridDim.y, bid = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
     for (int64_t i = bid * blockDim.x + threadIdx.x; i < status_words; i += nb * blockDim.x)
@@ -242,7 +242,7 @@ __global__ void k_sort_prep(SortCtl *ctl, SortSeg S, const int32_t *seg_off, int
 __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, SortSeg S,
     const int32_t *seg_off, int P, uint32_t *status, uint32_t *status_next, int64_t status_words, int pass,
-    const int *d_ib, int *d_err)
+    const int *d_ib, const int *d_kshift, int *d_err)
 {
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_excl[256];
@@ -291,9 +291,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     uint64_t *kout = sel ? keys0 : keys1;
     int32_t *vout = sel ? vals0 : vals1;
     // a non-trivial pass lies below bit 64 (the digits above are zero, so trivial)
-    const int ib = *d_ib;
-    const bool packed = ib != 0;
-    const int shift = ib + pass * 8;
+    const bool packed = *d_ib != 0;
+    const int shift = *d_kshift + pass * 8;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
 
@@ -462,9 +461,11 @@ int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *seg_off, int 
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "radix_sort: scratch");
     GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(SortCtl), ctx->stream));
     GCA_CUDA(ctx, cudaMemsetAsync(S.hist, 0, sizeof(uint32_t) * (size_t)P * 8 * 256, ctx->stream));
-    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(grid_for(max_seg_cap, kBlock * 8),
-                                                               ((int64_t)ctx->num_sms * 8 + P - 1) / P));
-    k_sort_hist<<<dim3(gx, P), kBlock, 0, ctx->stream>>>(sb.keys[0], seg_off, sb.d_ib, S, status, status_words);
+    // about 16 keys per thread in the largest segment (blocks past a smaller segment's end
+    // return at once), so uneven segments do not leave one segment's blocks looping
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(grid_for(max_seg_cap, kBlock * 16),
+                                                               ((int64_t)ctx->num_sms * 32 + P - 1) / P));
+    k_sort_hist<<<dim3(gx, P), kBlock, 0, ctx->stream>>>(sb.keys[0], seg_off, sb.d_kshift, S, status, status_words);
     GCA_CHECK_LAUNCH(ctx);
     k_sort_prep<<<P, 256, 0, ctx->stream>>>(ctl, S, seg_off, P, npasses, sb.d_sel);
     GCA_CHECK_LAUNCH(ctx);
@@ -473,7 +474,7 @@ int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *seg_off, int 
         GCA_PROF_BEGIN(ctx, kKidSortPass);
         k_sort_pass<<<(int)ntiles, kSortThreads, 0, ctx->stream>>>(
             sb.keys[0], sb.vals[0], sb.keys[1], sb.vals[1], ctl, S, seg_off, P, status + (p & 1) * status_words,
-            status + ((p + 1) & 1) * status_words, status_words, p, sb.d_ib, ctx->d_err);
+            status + ((p + 1) & 1) * status_words, status_words, p, sb.d_ib, sb.d_kshift, ctx->d_err);
         GCA_CHECK_LAUNCH(ctx);
         GCA_PROF_END(ctx, kKidSortPass);
     }

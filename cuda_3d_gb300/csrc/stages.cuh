@@ -98,8 +98,34 @@ int batch_alloc(gca3d_context *ctx, Batch &b, int P, int64_t cap, int64_t max_se
 // stage 0 of a scale: voxel downsample (voxel > 0) or gather copy into a batch
 // morton: output in Z-order of the voxels instead of the reference's (x, y, z) order
 // (same voxels, same centroids)
+// finer scales carried by a voxel stage: their voxel sizes, each half the previous one
+// (exactly, in float), so their cells refine the stage's cells (see k_voxel_keys)
+constexpr int kMaxSubLevels = 4;
+struct SubLevels
+{
+    int n = 0;
+    float voxel[kMaxSubLevels] = {0.0f, 0.0f, 0.0f, 0.0f};
+};
+
+// the sorted state of a voxel stage that finer scales refine instead of sorting again
+struct VoxelChain
+{
+    SortBuffers sb;          // the sort arrays (shared by the scales) and the last scale's view
+    const int32_t *in_off = nullptr;
+    int32_t *starts = nullptr, *d_m = nullptr; // the last scale's voxel runs
+    const KeyLayout *lay = nullptr;            // the last scale's key layout
+    int levels = 0, used = 0;
+    int P = 0;
+    int64_t total_cap = 0, max_seg_cap = 0;
+};
+
+// voxel-grid downsampling of P segments; morton: Z-order keys; finer (with morton):
+// carry the sub-cell bits of finer scales and record the sorted state in *chain, which
+// voxel_refine then turns into each finer scale's downsampling, in order
 int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap, int64_t max_seg_cap,
-                float voxel, Batch &out, bool morton = false);
+                float voxel, Batch &out, bool morton = false, const SubLevels *finer = nullptr,
+                VoxelChain *chain = nullptr);
+int voxel_refine(gca3d_context *ctx, const SegSrc *d_src, VoxelChain &chain, Batch &out);
 int gather_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t max_seg_cap, Batch &out,
                  bool with_normals);
 

@@ -98,8 +98,8 @@ __global__ void k_src_bounds(const SegSrc *src, int *ord)
 // segment index instead: the voxels then come out in Z-order, so runs of
 // consecutive output points are compact in space (the correspondence search of the
 // ICP stages a block's target cells once for such a run).
-__global__ void k_voxel_layout(const int *ord, int P, float voxel, bool morton, float3 *origin, KeyLayout *lay,
-                               int *d_err)
+__global__ void k_voxel_layout(const int *ord, int P, float voxel, bool morton, int sub_bits, float3 *origin,
+                               KeyLayout *lay, int *d_err)
 {
     __shared__ uint32_t s_max[3];
     if (threadIdx.x < 3)
@@ -138,13 +138,14 @@ __global__ void k_voxel_layout(const int *ord, int P, float voxel, bool morton, 
         L.total_bits = L.bseg + L.bx + L.by + L.bz;
         L.morton = 0;
         const int b = max(L.bx, max(L.by, L.bz));
-        if (morton && L.bseg + 3 * b <= 64)
+        if (morton && L.bseg + 3 * b + sub_bits <= 64)
         {
             L.bx = L.by = L.bz = b;
             L.total_bits = L.bseg + 3 * b;
             L.morton = 1;
         }
-        if (L.total_bits > 64)
+        // sub-cell bits for finer scales ride below a Z-order key
+        if (L.total_bits + sub_bits > 64 || (sub_bits && !L.morton))
             atomicOr(d_err, kErrKeyBits);
         *lay = L;
     }
@@ -163,15 +164,20 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v)
 }
 
 __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3 *origin, const KeyLayout *lay,
-                             float voxel, uint64_t *keys, int32_t *vals, int ib_cap, int *d_ib)
+                             float voxel, SubLevels sub, uint64_t *keys, int32_t *vals, int ib_cap, int *d_ib,
+                             int *d_kshift, int *d_err)
 {
     const int seg = blockIdx.y;
     const int n = *src[seg].d_n;
     const int base = off[seg];
     const KeyLayout L = *lay;
-    const int ib = packed_index_bits(L.total_bits, ib_cap);
+    const int sb = 3 * sub.n;
+    const int ib = packed_index_bits(L.total_bits + sb, ib_cap);
     if (seg == 0 && blockIdx.x == 0 && threadIdx.x == 0)
+    {
         *d_ib = ib;
+        *d_kshift = ib + sb;
+    }
     const float3 o = origin[seg];
     const float4 *pos = src[seg].pos;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -179,9 +185,22 @@ __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3
         float4 p = pos[i];
         uint64_t kx = (uint32_t)cell_of(p.x, o.x, voxel), ky = (uint32_t)cell_of(p.y, o.y, voxel),
                  kz = (uint32_t)cell_of(p.z, o.z, voxel);
-        const uint64_t key = ((uint64_t)seg << (L.bx + L.by + L.bz)) |
-                             (L.morton ? (spread3(kx) << 2) | (spread3(ky) << 1) | spread3(kz)
-                                       : (kx << (L.by + L.bz)) | (ky << L.bz) | kz);
+        uint64_t key = ((uint64_t)seg << (L.bx + L.by + L.bz)) |
+                       (L.morton ? (spread3(kx) << 2) | (spread3(ky) << 1) | spread3(kz)
+                                 : (kx << (L.by + L.bz)) | (ky << L.bz) | kz);
+        // each finer scale's cells, as that scale computes them: with its voxel half the
+        // previous one, its quotient is exactly twice the previous one, so each axis adds
+        // one bit (x, y, z -- the next three bits of the finer Z-order key)
+        for (int l = 0; l < sub.n; ++l)
+        {
+            const uint64_t fx = (uint32_t)cell_of(p.x, o.x, sub.voxel[l]), fy = (uint32_t)cell_of(p.y, o.y, sub.voxel[l]),
+                           fz = (uint32_t)cell_of(p.z, o.z, sub.voxel[l]);
+            const uint64_t bx = fx - 2 * kx, by = fy - 2 * ky, bz = fz - 2 * kz;
+            if ((bx | by | bz) > 1)
+                atomicOr(d_err, kErrInvalid);
+            key = (key << 3) | ((bx & 1) << 2) | ((by & 1) << 1) | (bz & 1);
+            kx = fx, ky = fy, kz = fz;
+        }
         sort_store(keys, vals, base + i, key, ib);
     }
 }
@@ -271,8 +290,125 @@ __global__ void k_voxel_reduce(const SegSrc *src, const int32_t *in_off, SortBuf
     }
 }
 
+// One finer scale from the previous one's sorted order: within each previous voxel's run
+// the elements are split, stably, by the next three sub-cell bits below the key, which
+// orders them by (finer key, index) -- what a full sort by the finer key gives.  One
+// thread per previous voxel (a handful of points each); the output goes to the other
+// buffer, and the finer scale's view and layout are written beside the previous ones.
+__global__ void k_voxel_refine(SortBuffers sb, const int32_t *starts, const int32_t *d_m, const KeyLayout *lay_in,
+                               int *d_sel_out, int *d_kshift_out, KeyLayout *lay_out)
+{
+    const int sel = *sb.d_sel;
+    const int ks = *sb.d_kshift - 3; // the finer key's lowest bit
+    const bool packed = *sb.d_ib != 0;
+    const uint64_t *kin = sb.keys[sel];
+    uint64_t *kout = sb.keys[sel ^ 1];
+    const int32_t *vin = sb.vals[sel];
+    int32_t *vout = sb.vals[sel ^ 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        *d_sel_out = sel ^ 1;
+        *d_kshift_out = ks;
+        KeyLayout L = *lay_in;
+        L.bx += 1, L.by += 1, L.bz += 1;
+        L.total_bits += 3;
+        *lay_out = L;
+    }
+    const int m = *d_m;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m; v += gridDim.x * blockDim.x)
+    {
+        const int s = starts[v], e = starts[v + 1];
+        int off[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int j = s; j < e; ++j)
+            ++off[(kin[j] >> ks) & 7];
+        int run = s;
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+        {
+            const int c = off[b];
+            off[b] = run;
+            run += c;
+        }
+        for (int j = s; j < e; ++j)
+        {
+            const uint64_t w = kin[j];
+            const int o = off[(w >> ks) & 7]++;
+            kout[o] = w;
+            if (!packed)
+                vout[o] = vin[j];
+        }
+    }
+}
+
+// the runs of equal keys (voxels) of the sorted view and their sums: the part of a voxel
+// stage after its order is known
+static int voxel_reduce_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap,
+                              const int32_t *in_off, const SortBuffers &sb, const KeyLayout *lay, Batch &out,
+                              int32_t *starts, int32_t *d_m)
+{
+    Arena &A = ctx->arena;
+    const int64_t cap = std::max<int64_t>(total_cap, 1);
+    int32_t *flags = A.get<int32_t>(cap);
+    int32_t *vid = A.get<int32_t>(cap);
+    int32_t *seg_count = A.get<int32_t>(P);
+    if (!flags || !vid || !seg_count)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "voxel_stage: scratch");
+    cudaStream_t s = ctx->stream;
+    const int32_t *d_n = in_off + P;
+    const int gs = std::min(grid_for(total_cap), ctx->num_sms * 8);
+    k_run_flags<<<gs, kBlock, 0, s>>>(sb, d_n, flags);
+    GCA_CHECK_LAUNCH(ctx);
+    int st = exclusive_scan(ctx, flags, vid, d_n, total_cap, d_m);
+    if (st)
+        return st;
+    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0xFF, sizeof(int32_t) * P, s));
+    k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts, sb, lay, seg_count);
+    GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_BEGIN(ctx, kKidVoxelReduce);
+    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col, ctx->d_err);
+    GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidVoxelReduce);
+    k_seg_first_to_offsets<<<1, 32, 0, s>>>(seg_count, P, d_m, out.seg_off);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+int voxel_refine(gca3d_context *ctx, const SegSrc *d_src, VoxelChain &c, Batch &out)
+{
+    if (c.used >= c.levels)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "voxel_refine: no finer scale carried");
+    Arena &A = ctx->arena;
+    const int64_t cap = std::max<int64_t>(c.total_cap, 1);
+    SortBuffers sb = c.sb;
+    sb.d_sel = A.get<int>(1);
+    sb.d_kshift = A.get<int>(1);
+    KeyLayout *lay = A.get<KeyLayout>(1);
+    int32_t *starts = A.get<int32_t>(cap + 1);
+    int32_t *d_m = A.get<int32_t>(1);
+    if (!sb.d_sel || !sb.d_kshift || !lay || !starts || !d_m)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "voxel_refine: scratch");
+    if (!out.pos)
+    {
+        int st = batch_alloc(ctx, out, c.P, c.total_cap, c.max_seg_cap, false, false);
+        if (st)
+            return st;
+    }
+    const int gs = std::min(grid_for(c.total_cap), ctx->num_sms * 8);
+    k_voxel_refine<<<gs, kBlock, 0, ctx->stream>>>(c.sb, c.starts, c.d_m, c.lay, sb.d_sel, sb.d_kshift, lay);
+    GCA_CHECK_LAUNCH(ctx);
+    int st = voxel_reduce_stage(ctx, d_src, c.P, c.total_cap, c.in_off, sb, lay, out, starts, d_m);
+    if (st)
+        return st;
+    c.sb = sb;
+    c.lay = lay;
+    c.starts = starts;
+    c.d_m = d_m;
+    c.used += 1;
+    return GCA3D_OK;
+}
+
 int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_cap, int64_t max_seg_cap,
-                float voxel, Batch &out, bool morton)
+                float voxel, Batch &out, bool morton, const SubLevels *finer, VoxelChain *chain)
 {
     if (!(voxel > 0.0f))
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "voxel size must be > 0");
@@ -289,14 +425,15 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     sb.vals[1] = A.get<int32_t>(cap);
     sb.d_sel = A.get<int>(1);
     sb.d_ib = A.get<int>(1);
-    int32_t *flags = A.get<int32_t>(cap);
-    int32_t *vid = A.get<int32_t>(cap);
+    sb.d_kshift = A.get<int>(1);
     int32_t *starts = A.get<int32_t>(cap + 1);
     int32_t *d_m = A.get<int32_t>(1);
-    int32_t *seg_count = A.get<int32_t>(P);
-    if (!in_off || !ord || !origin || !lay || !sb.keys[1] || !sb.vals[1] || !sb.d_sel || !sb.d_ib || !flags ||
-        !vid || !starts || !d_m || !seg_count)
+    if (!in_off || !ord || !origin || !lay || !sb.keys[1] || !sb.vals[1] || !sb.d_sel || !sb.d_ib || !sb.d_kshift ||
+        !starts || !d_m)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "voxel_stage: scratch");
+    const SubLevels sub = finer ? *finer : SubLevels{};
+    if (sub.n < 0 || sub.n > kMaxSubLevels || (sub.n && !morton))
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "voxel_stage: finer scales need Z-order keys");
     if (!out.pos)
     {
         int st = batch_alloc(ctx, out, P, total_cap, max_seg_cap, false, false);
@@ -311,30 +448,30 @@ int voxel_stage(gca3d_context *ctx, const SegSrc *d_src, int P, int64_t total_ca
     const int gx = std::min(grid_for(max_seg_cap, kBlock * 4), ctx->num_sms * 4);
     k_src_bounds<<<dim3(gx, P), kBlock, 0, s>>>(d_src, ord);
     GCA_CHECK_LAUNCH(ctx);
-    k_voxel_layout<<<1, 256, 0, s>>>(ord, P, voxel, morton, origin, lay, ctx->d_err);
+    k_voxel_layout<<<1, 256, 0, s>>>(ord, P, voxel, morton, 3 * sub.n, origin, lay, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
-    k_voxel_keys<<<dim3(gx, P), kBlock, 0, s>>>(d_src, in_off, origin, lay, voxel, sb.keys[0], sb.vals[0],
-                                                index_bits(cap), sb.d_ib);
+    k_voxel_keys<<<dim3(gx, P), kBlock, 0, s>>>(d_src, in_off, origin, lay, voxel, sub, sb.keys[0], sb.vals[0],
+                                                index_bits(cap), sb.d_ib, sb.d_kshift, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
-    const int32_t *d_n = in_off + P;
     int st = radix_sort(ctx, sb, in_off, P, total_cap, max_seg_cap, 64);
     if (st)
         return st;
-    const int gs = std::min(grid_for(total_cap), ctx->num_sms * 8);
-    k_run_flags<<<gs, kBlock, 0, s>>>(sb, d_n, flags);
-    GCA_CHECK_LAUNCH(ctx);
-    st = exclusive_scan(ctx, flags, vid, d_n, total_cap, d_m);
+    st = voxel_reduce_stage(ctx, d_src, P, total_cap, in_off, sb, lay, out, starts, d_m);
     if (st)
         return st;
-    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0xFF, sizeof(int32_t) * P, s));
-    k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts, sb, lay, seg_count);
-    GCA_CHECK_LAUNCH(ctx);
-    GCA_PROF_BEGIN(ctx, kKidVoxelReduce);
-    k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col, ctx->d_err);
-    GCA_CHECK_LAUNCH(ctx);
-    GCA_PROF_END(ctx, kKidVoxelReduce);
-    k_seg_first_to_offsets<<<1, 32, 0, s>>>(seg_count, P, d_m, out.seg_off);
-    GCA_CHECK_LAUNCH(ctx);
+    if (chain)
+    {
+        chain->sb = sb;
+        chain->in_off = in_off;
+        chain->starts = starts;
+        chain->d_m = d_m;
+        chain->lay = lay;
+        chain->levels = sub.n;
+        chain->used = 0;
+        chain->P = P;
+        chain->total_cap = total_cap;
+        chain->max_seg_cap = max_seg_cap;
+    }
     return GCA3D_OK;
 }
 

@@ -86,6 +86,9 @@ typedef struct {
     int nn_item_points;      /* source points per correspondence work item: 64, 128, 256 (default), 512 */
     int nn_blocks_per_sm;    /* correspondence grid = SMs x this (default 10), at most the items */
     int accum_blocks_per_sm; /* accumulate grid = SMs x this (default 6), at most the items */
+    int voxel_resort;        /* 1: sort every scale's voxels anew; 0 (default): where the next
+                                scales' voxel sizes halve exactly, one sort at the coarser scale
+                                carries their sub-cell bits and each finer scale splits its runs */
 } gca3d_tuning;
 
 typedef struct {

@@ -241,6 +241,28 @@ def test_autotune_and_every_launch_shape_give_identical_results(ctx, N, synth):
             assert a["iterations"] == b["iterations"]
 
 
+@pytest.mark.parametrize("voxels", [(0.04, 0.02, 0.01), (0.08, 0.04, 0.02, 0.01), (0.05, 0.02, 0.01)])
+def test_voxel_refinement_changes_no_bit(ctx, N, synth, voxels):
+    """Where the voxel sizes halve from scale to scale, one sort at the coarser scale
+    carries the finer scales' sub-cell bits and each finer scale only splits the coarser
+    voxels' runs; with voxel_resort every scale sorts anew.  Both give the same voxels in
+    the same order, so every result is bit-identical (0.05 -> 0.02 does not halve: a new
+    sort there, a refinement after it)."""
+    pairs = synth.batch_pairs(8, seed=4, n_min=20_000, n_max=80_000)
+    srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
+    tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
+    scales = [N.scale(v, 20, 1.5 * v, 2 * v, 2 * v) for v in voxels]
+    out = []
+    for resort in (0, 1):
+        prm = N.icp_params(scales, update_map=N.UPDATE_SE3_EXP, use_graph=True, tuning=N.Tuning(0, 0, 0, resort))
+        out.append(N.IcpPlan(ctx, srcs, tgts, prm).execute(results=True))
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a["T"], b["T"])
+        for k in ("iterations", "fitness", "inlier_rmse", "rmse_ref", "scale_iterations", "scale_n_src",
+                  "scale_n_tgt"):
+            assert a[k] == b[k], k
+
+
 def test_fp64_pose_routines_vs_cuda(ctx, N):
     """The pose update's short FP64 routines on this device, against CUDA: the Newton
     reciprocal within 1 ulp of IEEE division over 2^-60 .. 2^60, the small-angle
