@@ -739,7 +739,14 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
         else
             k_normals32<false><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
-        k_normals64<<<ctx->num_sms * 2, 128, 0, ctx->stream>>>(g.dev, normal_radius, max_nn, O);
+        // one warp per queued point and a long dependent FP64 chain per point: as many
+        // resident blocks as the registers allow, to overlap the chains
+        static const int blocks64 = [] {
+            int b = 0;
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_normals64, 128, 0) == cudaSuccess && b > 0 ? b
+                                                                                                            : 2;
+        }();
+        k_normals64<<<ctx->num_sms * blocks64, 128, 0, ctx->stream>>>(g.dev, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
     }
     if (do_grad && !do_normals)
