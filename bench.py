@@ -300,7 +300,8 @@ def run_ours(args):
         best, best_ms = N.icp_autotune(ctx, srcs, tgts, chosen, reps=2)
         chosen.tuning = best
         tuning = {"nn_item_points": best.nn_item_points, "nn_blocks_per_sm": best.nn_blocks_per_sm,
-                  "accum_blocks_per_sm": best.accum_blocks_per_sm, "ms_per_execute": best_ms,
+                  "accum_blocks_per_sm": best.accum_blocks_per_sm, "fused_finalize": best.fused_finalize,
+                  "ms_per_execute": best_ms,
                   "search_s": time.perf_counter() - t0}
     plan = N.IcpPlan(ctx, srcs, tgts, chosen)
     res_chosen = None

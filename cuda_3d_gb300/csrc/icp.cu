@@ -5,21 +5,23 @@
 // (src/registration/cuda_color_icp_build_least_square.cu:134-254) and
 // solve_JTJ_JTr<true> (src/registration/eigen_solver.hpp:44-85).
 //
-// Two launches per Gauss-Newton iteration cover every pair.  A block owns a chunk
-// of one pair's source points.  k_icp_nn transforms them by the pair's current pose
-// and finds the nearest target point inside max_corr (row-hashed grid, ties to the
-// smaller index); it keeps few registers so many warps hide the latency of the
-// neighbour walk, and it skips the walk for points whose certificate from an
-// earlier search of the scale still decides the answer (grid_query.cuh).  k_icp_accum builds the geometric and photometric residuals and
+// Three launches per Gauss-Newton iteration cover every pair (two with the fused
+// finalize).  A block owns a chunk of one pair's source points.  k_icp_nn transforms
+// them by the pair's current pose and finds the nearest target point inside max_corr
+// (row-hashed grid, ties to the smaller index); it keeps few registers so many warps
+// hide the latency of the neighbour walk, and it skips the walk for points whose
+// certificate from an earlier search of the scale still decides the answer
+// (grid_query.cuh).  k_icp_accum builds the geometric and photometric residuals and
 // their 6-vector Jacobians in FP32 and accumulates the 21 + 6 + 1 system terms plus
-// the correspondence count and squared distances.  Accumulation is compensated
-// FP32 inside the block (two-sum per thread and per shuffle level) and FP64 across
-// warps and blocks.  The last block of a pair to finish (atomic ticket, no
-// waiting) sums the pair's block partials in FP64 in block order, solves the 6x6
-// system by FP64 LDL^T, maps the step to SE(3) (Euler ZYX as the reference, or the
-// exponential), composes the pose in FP64 and applies the reference's
-// convergence test; a converged pair skips the remaining launches.  The source
-// cloud is never rewritten: the pose is applied on the fly.
+// the correspondence count and squared distances.  Accumulation is compensated FP32
+// inside the block (two-sum per thread and per shuffle level) and FP64 across warps
+// and blocks.  k_icp_finalize (one block per pair) -- or, fused, the last accumulate
+// block of the pair to finish (atomic ticket, no waiting) -- sums the pair's block
+// partials in FP64 in block order, solves the 6x6 system by FP64 LDL^T, maps the step
+// to SE(3) (Euler ZYX as the reference, or the exponential), composes the pose in
+// FP64 and applies the reference's convergence test; a converged pair skips the
+// remaining launches.  The source cloud is never rewritten: the pose is applied on
+// the fly.
 #include "grid_query.cuh"
 #include "icp.cuh"
 #include "pose_math.cuh"
@@ -241,7 +243,11 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
             S.rmse_ref = S.fitness = S.inlier_rmse = 0.0;
         }
     }
+    int nact = 0;
+    for (int p = 0; p < P; ++p)
+        nact += st[p].active;
     bmap[P] = b;
+    bmap[P + 1] = nact; // pairs the fused accumulate finalizes this iteration
     bmap_nn[P] = bn;
     bmap_nn[P + 1] = 0; // the correspondence kernel's work queue
 }
@@ -430,20 +436,249 @@ __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restr
     }
 }
 
-// step 2: residuals, Jacobians, block sums (one partial per block); three resident
-// blocks per SM (80 registers: the 30 sums and two points' gathers in flight)
+// one pair's finalize, by one whole block: the pair's block partials summed in FP64
+// in block order, the 6x6 solve, the step map, the FP64 pose update and the
+// reference's convergence test (color_icp.cu:216-228).  The partials are read from
+// L2: in the fused accumulate other blocks of the same launch wrote them.
 template <bool Comp>
+__device__ __noinline__ void finalize_pair(PairState *st, int P, int pair, const int *bmap, const double *partials,
+                                           IcpScale prm)
+{
+    PairState &Ps = st[pair];
+    __shared__ double s_red[kIcpThreads / 32][kTermsPad];
+    const int nb = Ps.nblocks, bstart = bmap[pair];
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    if (lane < kTerms)
+    {
+        constexpr int kW = kIcpThreads / 32;
+        const double *src = partials + (size_t)bstart * kTermsPad + lane;
+        if (Comp)
+        {
+            // four running sums (blocks grp + 8 (4 q + r), r = 0..3), added in a fixed order
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+            int j = grp;
+            for (; j + 3 * kW < nb; j += 4 * kW)
+            {
+                v0 += __ldcg(src + (size_t)j * kTermsPad);
+                v1 += __ldcg(src + (size_t)(j + kW) * kTermsPad);
+                v2 += __ldcg(src + (size_t)(j + 2 * kW) * kTermsPad);
+                v3 += __ldcg(src + (size_t)(j + 3 * kW) * kTermsPad);
+            }
+            for (; j < nb; j += kW)
+                v0 += __ldcg(src + (size_t)j * kTermsPad);
+            s_red[grp][lane] = (v0 + v1) + (v2 + v3);
+        }
+        else
+        {
+            float vf = 0.0f;
+            for (int j = grp; j < nb; j += kW)
+                vf += (float)__ldcg(src + (size_t)j * kTermsPad);
+            s_red[grp][lane] = (double)vf;
+        }
+    }
+    __syncthreads();
+    __shared__ double s_S[kTermsPad];
+    if (threadIdx.x < kTerms)
+    {
+        const int k = threadIdx.x;
+        double v = 0.0;
+        float vf = 0.0f;
+        for (int w = 0; w < kIcpThreads / 32; ++w)
+        {
+            if (Comp)
+                v += s_red[w][k];
+            else
+                vf += (float)s_red[w][k];
+        }
+        s_S[k] = Comp ? v : (double)vf;
+    }
+    __syncthreads();
+    const int warp = grp;
+    if (warp == 0)
+    {
+        // solve, step map and composition over the lanes of warp 0
+        double x[6];
+        const int singular = solve6_warp(s_S, x);
+        const double Ti = pose_from_x_warp(x, prm.update_map); // lanes 0..15: Ti[lane]
+        const int r = (lane >> 2) & 3, c = lane & 3;
+        const double Told = lane < 16 ? Ps.T[lane] : 0.0;
+        double v = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            v += __shfl_sync(0xffffffffu, Ti, 4 * r + k) * __shfl_sync(0xffffffffu, Told, 4 * k + c);
+        const double t00 = __shfl_sync(0xffffffffu, Ti, 0), t11 = __shfl_sync(0xffffffffu, Ti, 5),
+                     t22 = __shfl_sync(0xffffffffu, Ti, 10), t03 = __shfl_sync(0xffffffffu, Ti, 3),
+                     t13 = __shfl_sync(0xffffffffu, Ti, 7), t23 = __shfl_sync(0xffffffffu, Ti, 11);
+        const int iters = Ps.iters;
+        if (prm.trace && iters < prm.trace_cap)
+        {
+            IcpTrace &tr = prm.trace[(size_t)iters * P + pair];
+            if (lane < 16)
+                tr.T[lane] = Told;
+            if (lane < kTerms)
+                tr.S[lane] = s_S[lane];
+            if (lane == 0)
+            {
+#pragma unroll
+                for (int q = 0; q < 6; ++q)
+                    tr.x[q] = x[q];
+                tr.status = singular;
+            }
+        }
+        __syncwarp();
+        if (lane < 16)
+            Ps.T[lane] = v;
+        if (lane == 0)
+        {
+            if (s_S[28] == 0.0)
+                Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
+            else if (singular && Ps.status == 0)
+                Ps.status = GCA3D_ERR_SINGULAR;
+            Ps.iters = iters + 1;
+            Ps.scale_iters[Ps.scale] += 1;
+            Ps.nn_warm = 1;
+            const double cth = 0.5 * (t00 + t11 + t22 - 1.0);
+            const double tsq = t03 * t03 + t13 * t13 + t23 * t23;
+            if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
+            {
+                Ps.converged = 1;
+                Ps.active = 0;
+            }
+        }
+    }
+    else if (warp == 1)
+    {
+        // the statistics, on their own warp (one division per lane)
+        const double ns = (double)Ps.nsrc;
+        const int m = lane % 3;
+        const double num = m == 0 ? s_S[27] : (m == 1 ? s_S[28] : s_S[29]);
+        const double den = m == 2 ? s_S[28] : ns;
+        double q = num / den;
+        if (m == 2)
+            q = s_S[28] > 0.0 ? sqrt(q) : 0.0;
+        if (lane == 0)
+            Ps.rmse_ref = q;
+        else if (lane == 1)
+            Ps.fitness = q;
+        else if (lane == 2)
+            Ps.inlier_rmse = q;
+    }
+}
+
+// the work maps over the pairs still active (the next iteration's NN and accumulate
+// launches get no items for converged pairs), their count and, in a captured
+// schedule, the loop condition.  Run by one whole block once every pair of the
+// iteration is finalized.
+__device__ __noinline__ void rebuild_maps(PairState *st, int P, int *bmap, int *bmap_nn, IcpLoop loop)
+{
+    __shared__ int s_sum[kIcpThreads], s_sum_nn[kIcpThreads];
+    __shared__ int s_nact;
+    if (threadIdx.x == 0)
+        s_nact = 0;
+    __syncthreads();
+    const int per = (P + kIcpThreads - 1) / kIcpThreads;
+    const int p0 = min(P, (int)threadIdx.x * per), p1 = min(P, p0 + per);
+    int a = 0, an = 0, na = 0;
+    for (int q = p0; q < p1; ++q)
+        if (__ldcg(&st[q].active))
+        {
+            a += st[q].nblocks;
+            an += st[q].nblocks_nn;
+            ++na;
+        }
+    if (na)
+        atomicAdd(&s_nact, na);
+    s_sum[threadIdx.x] = a;
+    s_sum_nn[threadIdx.x] = an;
+    __syncthreads();
+    if (threadIdx.x < 32)
+    {
+        // exclusive prefix of the 256 per-thread sums: 8 per lane, then across the warp
+        const int l = threadIdx.x;
+        int va[kIcpThreads / 32], vn[kIcpThreads / 32], sa = 0, sn = 0;
+#pragma unroll
+        for (int k = 0; k < kIcpThreads / 32; ++k)
+        {
+            va[k] = s_sum[l * (kIcpThreads / 32) + k];
+            vn[k] = s_sum_nn[l * (kIcpThreads / 32) + k];
+            sa += va[k];
+            sn += vn[k];
+        }
+        int ia = sa, in = sn;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int ya = __shfl_up_sync(0xffffffffu, ia, o), yn = __shfl_up_sync(0xffffffffu, in, o);
+            if (l >= o)
+                ia += ya, in += yn;
+        }
+        int ra = ia - sa, rn = in - sn;
+#pragma unroll
+        for (int k = 0; k < kIcpThreads / 32; ++k)
+        {
+            s_sum[l * (kIcpThreads / 32) + k] = ra;
+            s_sum_nn[l * (kIcpThreads / 32) + k] = rn;
+            ra += va[k];
+            rn += vn[k];
+        }
+        if (l == 31)
+        {
+            bmap[P] = ra;
+            bmap[P + 1] = s_nact;
+            bmap_nn[P] = rn;
+            bmap_nn[P + 1] = 0;
+            *loop.ticket = 0u;
+            if (loop.iter)
+            {
+                const int it = ++(*loop.iter);
+                cudaGraphSetConditional(loop.handle, (rn > 0 && it < loop.max_iter) ? 1u : 0u);
+            }
+        }
+    }
+    __syncthreads();
+    a = s_sum[threadIdx.x];
+    an = s_sum_nn[threadIdx.x];
+    for (int q = p0; q < p1; ++q)
+    {
+        bmap[q] = a;
+        bmap_nn[q] = an;
+        if (__ldcg(&st[q].active))
+        {
+            a += st[q].nblocks;
+            an += st[q].nblocks_nn;
+        }
+    }
+}
+
+// step 2: residuals, Jacobians, block sums (one partial per block); three resident
+// blocks per SM (80 registers: the 30 sums and two points' gathers in flight).
+// Fused: after storing its partial a block takes the pair's ticket, and the pair's
+// last block runs the pair's finalize; the last pair to be finalized rebuilds the
+// work maps.  A block that starts after that rebuild finds no item: within a scale
+// the active set only shrinks, so the next item count is at most this one, and every
+// block below this count has work left until the rebuild.
+template <bool Comp, bool Fused>
 __global__ void __launch_bounds__(kIcpThreads, 3) k_icp_accum(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                            const float4 *__restrict__ tpos,
                                                            const float4 *__restrict__ attr0,
                                                            const float4 *__restrict__ attr1,
-                                                           const int2 *__restrict__ corr, const PairState *st,
-                                                           const int *bmap, int P, double *partials, float slg,
-                                                           float slc, const int32_t *d_nt, int *err)
+                                                           const int2 *__restrict__ corr, PairState *st,
+                                                           int *bmap, int *bmap_nn, int P, double *partials,
+                                                           float slg, float slc, const int32_t *d_nt, int *err,
+                                                           IcpScale prm, IcpLoop loop)
 {
     __shared__ int s_pair;
     __shared__ float s_T[12];
+    __shared__ int s_fin;
     const int items = bmap[P];
+    const int nact = Fused ? bmap[P + 1] : 0;
+    if (Fused && items == 0)
+    {
+        // no active pair: nothing to finalize, but the maps and the loop condition are set
+        if (blockIdx.x == 0)
+            rebuild_maps(st, P, bmap, bmap_nn, loop);
+        return;
+    }
     for (int w = blockIdx.x; w < items; w += gridDim.x)
     {
     const BlockPair b = item_pair(w, src_off, st, bmap, P, kIcpChunk, s_T, &s_pair);
@@ -487,145 +722,44 @@ __global__ void __launch_bounds__(kIcpThreads, 3) k_icp_accum(const float4 *__re
         }
     }
     block_reduce_store<Comp>(acc, partials + (size_t)w * kTermsPad);
+    if (Fused)
+    {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0)
+            s_fin = atomicAdd(&st[b.pair].ticket, 1u) == (unsigned)(st[b.pair].nblocks - 1);
+        __syncthreads();
+        if (s_fin)
+        {
+            __threadfence();
+            finalize_pair<Comp>(st, P, b.pair, bmap, partials, prm);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                st[b.pair].ticket = 0u;
+                s_fin = P == 1 || atomicAdd(loop.ticket, 1u) == (unsigned)(nact - 1);
+            }
+            __syncthreads();
+            if (s_fin)
+            {
+                __threadfence();
+                rebuild_maps(st, P, bmap, bmap_nn, loop);
+            }
+        }
+    }
     }
 }
 
-// step 3, one block per pair: the pair's block partials summed in FP64 in block
-// order, the 6x6 solve, the step map, the FP64 pose update and the reference's
-// convergence test (color_icp.cu:216-228).  With a loop, the last block to finish
-// decides whether the device-side iteration loop goes on: while a pair is active
-// and the scale's budget lasts.
+// the finalize as a launch of its own (one block per pair); the last block to
+// finish rebuilds the work maps
 template <bool Comp>
 __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int P, int *bmap, int *bmap_nn,
                                                               const double *partials, IcpScale prm, IcpLoop loop)
 {
-    const int pair = blockIdx.x;
-    PairState &Ps = st[pair];
-    __shared__ double s_red[kIcpThreads / 32][kTermsPad];
     __shared__ int s_last;
-    if (Ps.active)
-    {
-        const int nb = Ps.nblocks, bstart = bmap[pair];
-        const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
-        if (lane < kTerms)
-        {
-            constexpr int kW = kIcpThreads / 32;
-            const double *src = partials + (size_t)bstart * kTermsPad + lane;
-            if (Comp)
-            {
-                // four running sums (blocks grp + 8 (4 q + r), r = 0..3), added in a fixed order
-                double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
-                int j = grp;
-                for (; j + 3 * kW < nb; j += 4 * kW)
-                {
-                    v0 += src[(size_t)j * kTermsPad];
-                    v1 += src[(size_t)(j + kW) * kTermsPad];
-                    v2 += src[(size_t)(j + 2 * kW) * kTermsPad];
-                    v3 += src[(size_t)(j + 3 * kW) * kTermsPad];
-                }
-                for (; j < nb; j += kW)
-                    v0 += src[(size_t)j * kTermsPad];
-                s_red[grp][lane] = (v0 + v1) + (v2 + v3);
-            }
-            else
-            {
-                float vf = 0.0f;
-                for (int j = grp; j < nb; j += kW)
-                    vf += (float)src[(size_t)j * kTermsPad];
-                s_red[grp][lane] = (double)vf;
-            }
-        }
-        __syncthreads();
-        __shared__ double s_S[kTermsPad];
-        if (threadIdx.x < kTerms)
-        {
-            const int k = threadIdx.x;
-            double v = 0.0;
-            float vf = 0.0f;
-            for (int w = 0; w < kIcpThreads / 32; ++w)
-            {
-                if (Comp)
-                    v += s_red[w][k];
-                else
-                    vf += (float)s_red[w][k];
-            }
-            s_S[k] = Comp ? v : (double)vf;
-        }
-        __syncthreads();
-        const int warp = grp;
-        if (warp == 0)
-        {
-            // solve, step map and composition over the lanes of warp 0
-            double x[6];
-            const int singular = solve6_warp(s_S, x);
-            const double Ti = pose_from_x_warp(x, prm.update_map); // lanes 0..15: Ti[lane]
-            const int r = (lane >> 2) & 3, c = lane & 3;
-            const double Told = lane < 16 ? Ps.T[lane] : 0.0;
-            double v = 0.0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                v += __shfl_sync(0xffffffffu, Ti, 4 * r + k) * __shfl_sync(0xffffffffu, Told, 4 * k + c);
-            const double t00 = __shfl_sync(0xffffffffu, Ti, 0), t11 = __shfl_sync(0xffffffffu, Ti, 5),
-                         t22 = __shfl_sync(0xffffffffu, Ti, 10), t03 = __shfl_sync(0xffffffffu, Ti, 3),
-                         t13 = __shfl_sync(0xffffffffu, Ti, 7), t23 = __shfl_sync(0xffffffffu, Ti, 11);
-            const int iters = Ps.iters;
-            if (prm.trace && iters < prm.trace_cap)
-            {
-                IcpTrace &tr = prm.trace[(size_t)iters * P + pair];
-                if (lane < 16)
-                    tr.T[lane] = Told;
-                if (lane < kTerms)
-                    tr.S[lane] = s_S[lane];
-                if (lane == 0)
-                {
-#pragma unroll
-                    for (int q = 0; q < 6; ++q)
-                        tr.x[q] = x[q];
-                    tr.status = singular;
-                }
-            }
-            __syncwarp();
-            if (lane < 16)
-                Ps.T[lane] = v;
-            if (lane == 0)
-            {
-                if (s_S[28] == 0.0)
-                    Ps.status = GCA3D_ERR_NO_CORRESPONDENCES;
-                else if (singular && Ps.status == 0)
-                    Ps.status = GCA3D_ERR_SINGULAR;
-                Ps.iters = iters + 1;
-                Ps.scale_iters[Ps.scale] += 1;
-                Ps.nn_warm = 1;
-                const double cth = 0.5 * (t00 + t11 + t22 - 1.0);
-                const double tsq = t03 * t03 + t13 * t13 + t23 * t23;
-                if (cth >= 1.0 - prm.rot_eps && tsq <= prm.trans_eps)
-                {
-                    Ps.converged = 1;
-                    Ps.active = 0;
-                }
-            }
-        }
-        else if (warp == 1)
-        {
-            // the statistics, on their own warp (one division per lane)
-            const double ns = (double)Ps.nsrc;
-            const int m = lane % 3;
-            const double num = m == 0 ? s_S[27] : (m == 1 ? s_S[28] : s_S[29]);
-            const double den = m == 2 ? s_S[28] : ns;
-            double q = num / den;
-            if (m == 2)
-                q = s_S[28] > 0.0 ? sqrt(q) : 0.0;
-            if (lane == 0)
-                Ps.rmse_ref = q;
-            else if (lane == 1)
-                Ps.fitness = q;
-            else if (lane == 2)
-                Ps.inlier_rmse = q;
-        }
-    }
-    // the last block: work maps over the pairs still active (the next iteration's
-    // NN and accumulate launches get no items for converged pairs) and, in a
-    // captured schedule, the loop condition
+    if (st[blockIdx.x].active)
+        finalize_pair<Comp>(st, P, blockIdx.x, bmap, partials, prm);
     if (gridDim.x > 1)
     {
         __threadfence();
@@ -638,75 +772,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
     __syncthreads();
     if (!s_last)
         return;
-    __shared__ int s_sum[kIcpThreads], s_sum_nn[kIcpThreads];
-    const int per = (P + kIcpThreads - 1) / kIcpThreads;
-    const int p0 = min(P, (int)threadIdx.x * per), p1 = min(P, p0 + per);
-    int a = 0, an = 0;
-    for (int q = p0; q < p1; ++q)
-        if (__ldcg(&st[q].active))
-        {
-            a += st[q].nblocks;
-            an += st[q].nblocks_nn;
-        }
-    s_sum[threadIdx.x] = a;
-    s_sum_nn[threadIdx.x] = an;
-    __syncthreads();
-    if (threadIdx.x < 32)
-    {
-        // exclusive prefix of the 256 per-thread sums: 8 per lane, then across the warp
-        const int l = threadIdx.x;
-        int va[kIcpThreads / 32], vn[kIcpThreads / 32], sa = 0, sn = 0;
-#pragma unroll
-        for (int k = 0; k < kIcpThreads / 32; ++k)
-        {
-            va[k] = s_sum[l * (kIcpThreads / 32) + k];
-            vn[k] = s_sum_nn[l * (kIcpThreads / 32) + k];
-            sa += va[k];
-            sn += vn[k];
-        }
-        int ia = sa, in = sn;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const int ya = __shfl_up_sync(0xffffffffu, ia, o), yn = __shfl_up_sync(0xffffffffu, in, o);
-            if (l >= o)
-                ia += ya, in += yn;
-        }
-        int ra = ia - sa, rn = in - sn;
-#pragma unroll
-        for (int k = 0; k < kIcpThreads / 32; ++k)
-        {
-            s_sum[l * (kIcpThreads / 32) + k] = ra;
-            s_sum_nn[l * (kIcpThreads / 32) + k] = rn;
-            ra += va[k];
-            rn += vn[k];
-        }
-        if (l == 31)
-        {
-            bmap[P] = ra;
-            bmap_nn[P] = rn;
-            bmap_nn[P + 1] = 0;
-            *loop.ticket = 0u;
-            if (loop.iter)
-            {
-                const int it = ++(*loop.iter);
-                cudaGraphSetConditional(loop.handle, (rn > 0 && it < loop.max_iter) ? 1u : 0u);
-            }
-        }
-    }
-    __syncthreads();
-    a = s_sum[threadIdx.x];
-    an = s_sum_nn[threadIdx.x];
-    for (int q = p0; q < p1; ++q)
-    {
-        bmap[q] = a;
-        bmap_nn[q] = an;
-        if (__ldcg(&st[q].active))
-        {
-            a += st[q].nblocks;
-            an += st[q].nblocks_nn;
-        }
-    }
+    rebuild_maps(st, P, bmap, bmap_nn, loop);
 }
 
 IcpShape icp_shape(const gca3d_tuning &t)
@@ -718,6 +784,7 @@ IcpShape icp_shape(const gca3d_tuning &t)
         s.nn_bps = std::min(t.nn_blocks_per_sm, 64);
     if (t.accum_blocks_per_sm > 0)
         s.acc_bps = std::min(t.accum_blocks_per_sm, 64);
+    s.fused = t.fused_finalize != 0;
     return s;
 }
 
@@ -751,20 +818,38 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
     k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
                                                        corr, cert, nn_out, shape.nn_chunk, bmap_nn + src.P + 1);
     GCA_CHECK_LAUNCH(ctx);
-    if (compensated)
-        k_icp_accum<true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
-                                                                     corr, st, bmap, src.P, partials, prm.sqrt_lg,
-                                                                     prm.sqrt_lc, g.dev.d_n, ctx->d_err);
+    const int32_t *d_nt = g.dev.d_n;
+    if (shape.fused)
+    {
+        if (compensated)
+            k_icp_accum<true, true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(
+                src.pos, src.seg_off, g.dev.spos, attr0, attr1, corr, st, bmap, bmap_nn, src.P, partials,
+                prm.sqrt_lg, prm.sqrt_lc, d_nt, ctx->d_err, prm, loop);
+        else
+            k_icp_accum<false, true><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(
+                src.pos, src.seg_off, g.dev.spos, attr0, attr1, corr, st, bmap, bmap_nn, src.P, partials,
+                prm.sqrt_lg, prm.sqrt_lc, d_nt, ctx->d_err, prm, loop);
+        GCA_CHECK_LAUNCH(ctx);
+    }
     else
-        k_icp_accum<false><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev.spos, attr0, attr1,
-                                                                      corr, st, bmap, src.P, partials, prm.sqrt_lg,
-                                                                      prm.sqrt_lc, g.dev.d_n, ctx->d_err);
-    GCA_CHECK_LAUNCH(ctx);
-    if (compensated)
-        k_icp_finalize<true><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm, loop);
-    else
-        k_icp_finalize<false><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm, loop);
-    GCA_CHECK_LAUNCH(ctx);
+    {
+        if (compensated)
+            k_icp_accum<true, false><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(
+                src.pos, src.seg_off, g.dev.spos, attr0, attr1, corr, st, bmap, bmap_nn, src.P, partials,
+                prm.sqrt_lg, prm.sqrt_lc, d_nt, ctx->d_err, prm, loop);
+        else
+            k_icp_accum<false, false><<<grid_acc, kIcpThreads, 0, ctx->stream>>>(
+                src.pos, src.seg_off, g.dev.spos, attr0, attr1, corr, st, bmap, bmap_nn, src.P, partials,
+                prm.sqrt_lg, prm.sqrt_lc, d_nt, ctx->d_err, prm, loop);
+        GCA_CHECK_LAUNCH(ctx);
+        if (compensated)
+            k_icp_finalize<true><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm,
+                                                                         loop);
+        else
+            k_icp_finalize<false><<<src.P, kIcpThreads, 0, ctx->stream>>>(st, src.P, bmap, bmap_nn, partials, prm,
+                                                                          loop);
+        GCA_CHECK_LAUNCH(ctx);
+    }
     GCA_PROF_END(ctx, kKidIcpIter);
     return GCA3D_OK;
 }

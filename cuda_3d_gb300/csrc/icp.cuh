@@ -19,6 +19,7 @@ struct IcpShape
     int nn_chunk = kNNChunk;
     int nn_bps = 10;
     int acc_bps = 6;
+    bool fused = false; // the accumulate's last block of each pair finalizes it
 };
 IcpShape icp_shape(const gca3d_tuning &t);
 constexpr int kTerms = 30;      // 21 JTJ (upper) + 6 JTr + r^2 + correspondences + sum d^2
@@ -65,10 +66,11 @@ struct IcpScale
     int trace_cap = 0;
 };
 
-// control of one iteration: the finalize kernel's blocks take a ticket (zero
-// before the first iteration); the last one rebuilds the work maps and, in a
-// captured schedule (iter set), counts the iteration and sets the WHILE node's
-// condition
+// control of one iteration: each finalized pair takes a ticket (zero before the
+// first iteration); the last one rebuilds the work maps and, in a captured
+// schedule (iter set), counts the iteration and sets the WHILE node's condition.
+// The maps are bmap[P + 2] (item offsets, total, active pairs) and bmap_nn[P + 2]
+// (item offsets, total, work queue).
 struct IcpLoop
 {
     cudaGraphConditionalHandle handle = 0;

@@ -176,7 +176,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         int2 *corr = ctx->arena.get<int2>(std::max<int64_t>(bs.cap, 1));
         const NNCerts cert{ctx->arena.get<float4>(std::max<int64_t>(bs.cap, 1)),
                            ctx->arena.get<int>(std::max<int64_t>(bs.cap, 1))};
-        int *bmap = ctx->arena.get<int>(P + 1);
+        int *bmap = ctx->arena.get<int>(P + 2); // offsets, total, active pairs
         int *bmap_nn = ctx->arena.get<int>(P + 2); // offsets, total, work queue
         float4 *nrm_b = own_nn_grid && !keep ? ctx->arena.get<float4>(g.cap) : nullptr;
         float4 *grd_b = own_nn_grid ? ctx->arena.get<float4>(g.cap) : nullptr;
@@ -577,7 +577,8 @@ int gca3d_color_icp(gca3d_context *ctx, gca3d_cloud *src, gca3d_cloud *tgt, cons
 } // extern "C"
 
 // ---------------------------------------------------------------------------
-// launch-shape autotuner: coordinate descent over the knobs of gca3d_tuning, each
+// launch-shape autotuner: coordinate descent over the launch-shape knobs of
+// gca3d_tuning (item size, the two grids, the finalize's own launch or not), each
 // candidate timed on the caller's workload as a fresh plan (one warm-up execute,
 // then `reps` executes between CUDA events on the context stream)
 // ---------------------------------------------------------------------------
@@ -589,7 +590,7 @@ extern "C" int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *
     reps = std::max(reps, 1);
     gca3d_icp_params p = *params;
     const IcpShape s0 = icp_shape(p.tuning);
-    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps, p.tuning.voxel_resort};
+    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps, p.tuning.voxel_resort, s0.fused ? 1 : 0};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     {
@@ -631,14 +632,17 @@ extern "C" int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *
     const int nn_items[] = {64, 128, 256, 512};
     const int nn_bps[] = {4, 6, 8, 10, 14, 20};
     const int acc_bps[] = {2, 3, 4, 6, 8, 12};
-    for (int knob = 0; knob < 3 && !st; ++knob)
+    const int fused[] = {0, 1};
+    for (int knob = 0; knob < 4 && !st; ++knob)
     {
-        const int *vals = knob == 0 ? nn_items : (knob == 1 ? nn_bps : acc_bps);
-        const int nv = knob == 0 ? 4 : 6;
+        const int *vals = knob == 0 ? nn_items : (knob == 1 ? nn_bps : (knob == 2 ? acc_bps : fused));
+        const int nv = knob == 0 ? 4 : (knob == 3 ? 2 : 6);
         for (int v = 0; v < nv && !st; ++v)
         {
             gca3d_tuning t = cur;
-            int &field = knob == 0 ? t.nn_item_points : (knob == 1 ? t.nn_blocks_per_sm : t.accum_blocks_per_sm);
+            int &field = knob == 0 ? t.nn_item_points
+                                   : (knob == 1 ? t.nn_blocks_per_sm
+                                                : (knob == 2 ? t.accum_blocks_per_sm : t.fused_finalize));
             if (field == vals[v])
                 continue;
             field = vals[v];

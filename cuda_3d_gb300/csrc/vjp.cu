@@ -296,7 +296,7 @@ extern "C" int gca3d_color_icp_vjp(gca3d_context *ctx, gca3d_cloud *src, gca3d_c
     float4 *attr0 = ctx->arena.get<float4>(g.cap);
     float4 *attr1 = ctx->arena.get<float4>(g.cap);
     PairState *pst = ctx->arena.get<PairState>(1);
-    int *bmap = ctx->arena.get<int>(2);
+    int *bmap = ctx->arena.get<int>(3);
     int *bmap_nn = ctx->arena.get<int>(3);
     double *partials = ctx->arena.get<double>((size_t)max_blocks * kTermsPad);
     int2 *corr = ctx->arena.get<int2>((size_t)(K + 1) * src->capacity);

@@ -89,6 +89,8 @@ typedef struct {
     int voxel_resort;        /* 1: sort every scale's voxels anew; 0 (default): where the next
                                 scales' voxel sizes halve exactly, one sort at the coarser scale
                                 carries their sub-cell bits and each finer scale splits its runs */
+    int fused_finalize;      /* 1: the last accumulate block of each pair runs the pair's solve and
+                                pose update; 0 (default): they are a launch of their own */
 } gca3d_tuning;
 
 typedef struct {

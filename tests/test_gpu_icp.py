@@ -233,12 +233,52 @@ def test_autotune_and_every_launch_shape_give_identical_results(ctx, N, synth):
     assert best.nn_item_points in (64, 128, 256, 512)
     assert best.nn_blocks_per_sm > 0 and best.accum_blocks_per_sm > 0 and ms > 0
     ref = N.IcpPlan(ctx, srcs, tgts, prm).execute(results=True)
-    for tune in (best, N.Tuning(64, 4, 2), N.Tuning(512, 20, 12)):
+    for tune in (best, N.Tuning(64, 4, 2), N.Tuning(512, 20, 12), N.Tuning(128, 6, 3, 0, 1)):
         p2 = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=True, tuning=tune)
         got = N.IcpPlan(ctx, srcs, tgts, p2).execute(results=True)
         for a, b in zip(ref, got):
             np.testing.assert_array_equal(a["T"], b["T"])
             assert a["iterations"] == b["iterations"]
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+@pytest.mark.parametrize("compensated", [True, False])
+def test_fused_and_separate_finalize_agree(ctx, N, synth, use_graph, compensated):
+    """The finalize run by each pair's last accumulate block and as a launch of its
+    own (default) give the same bits: the same partials summed in the same order, the
+    same solve.  Pairs converge at different iterations, so the fused path also
+    rebuilds the work maps while other pairs are still accumulating."""
+    pairs = synth.batch_pairs(12, seed=5, n_min=10_000, n_max=90_000)
+    srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
+    tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
+    out = []
+    for fused in (0, 1):
+        prm = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=use_graph, compensated=compensated,
+                           tuning=N.Tuning(0, 0, 0, 0, fused))
+        out.append(N.IcpPlan(ctx, srcs, tgts, prm).execute(results=True))
+    iters = set()
+    for a, b in zip(*out):
+        np.testing.assert_array_equal(a["T"], b["T"])
+        for k in ("iterations", "converged", "status", "fitness", "inlier_rmse", "rmse_ref", "scale_iterations"):
+            assert a[k] == b[k], k
+        iters.add(tuple(a["scale_iterations"]))
+    assert len(iters) > 1  # the pairs stop at different iterations
+    # a single pair (its last block is the last of the iteration), an empty source
+    # alone (no item at all: the iteration still ends the loop) and beside others
+    empty = ctx.cloud(100)
+    cases = [([srcs[0]], [tgts[0]]), ([empty], [tgts[0]]), ([srcs[1], empty, srcs[2]], tgts[1:4])]
+    for cs, ct in cases:
+        got = []
+        for fused in (0, 1):
+            prm = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=use_graph,
+                               compensated=compensated, tuning=N.Tuning(0, 0, 0, 0, fused))
+            got.append(N.IcpPlan(ctx, cs, ct, prm).execute(results=True))
+        for a, b in zip(*got):
+            np.testing.assert_array_equal(a["T"], b["T"])
+            assert a["iterations"] == b["iterations"] and a["status"] == b["status"]
+        for r, c in zip(got[0], cs):
+            if c is empty:
+                assert r["status"] == N.ERR_NO_CORRESPONDENCES and r["iterations"] == 0
 
 
 @pytest.mark.parametrize("voxels", [(0.04, 0.02, 0.01), (0.08, 0.04, 0.02, 0.01), (0.05, 0.02, 0.01)])
