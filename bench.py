@@ -366,14 +366,18 @@ def run_ours(args):
     plans = [plan, N.IcpPlan(ctx, sets[1][0], sets[1][1], chosen)]
 
     def run_e2e(steps):
+        # step k+1 is queued behind step k before step k's results are read, so the
+        # GPU never waits for the host; a set is refilled once its plan's results are in
         upload(0)
+        stream.wait_event(up_events[0])
+        plans[0].execute(results=False)
         out = None
         for k in range(steps):
             cur = k & 1
-            stream.wait_event(up_events[cur])
-            plans[cur].execute(results=False)
             if k + 1 < steps:
-                upload(cur ^ 1)  # the other set's last plan run has been read back
+                upload(cur ^ 1)  # step k-1 used this set and has been read back
+                stream.wait_event(up_events[cur ^ 1])
+                plans[cur ^ 1].execute(results=False)
             out = plans[cur].results()
         return out
 
@@ -385,12 +389,13 @@ def run_ours(args):
     torch.cuda.synchronize()
     ms_e2e = reduce_max((time.perf_counter() - t0) * 1e3 / args.steps, "cuda")
     barrier()
-    d2h = P * 184  # the pair states read back per step (sizeof PairState)
+    d2h = plan.readback_bytes()  # the pair states and the error word read back per step
     same = all(np.array_equal(a["T"], b["T"]) for a, b in zip(res_e2e, res_chosen))
     e2e = {"value": world * P / (ms_e2e / 1000.0), "unit": "pairs/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e, "results_equal_resident_run": same,
            "pipeline": "two cloud sets and plans; step k+1's upload (second context's stream, copy-engine "
-                       "mode) overlaps step k's registration; host wall clock with a device synchronize on both "
+                       "mode) overlaps step k's registration and step k+1 is queued before step k's results are "
+                       "read; host wall clock with a device synchronize on both "
                        "sides"}
 
     # ---- roofline of the ICP iteration kernel (eager run, CUDA events) ---------

@@ -82,6 +82,13 @@ int consume_device_error(gca3d_context *ctx, const char *where)
     if (!h)
         return GCA3D_OK;
     GCA_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    return device_error_status(ctx, h, where);
+}
+
+int device_error_status(gca3d_context *ctx, int h, const char *where)
+{
+    if (!h)
+        return GCA3D_OK;
     if (h & kErrTimeout)
         return fail(ctx, GCA3D_ERR_TIMEOUT, std::string(where) + ": a look-back wait gave up");
     if (h & kErrKeyBits)

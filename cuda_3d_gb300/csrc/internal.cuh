@@ -177,6 +177,8 @@ inline int grid_for(int64_t n, int per_block = kBlock)
 int ensure_attr(gca3d_context *ctx, gca3d_cloud *c, bool normals, bool grad);
 // reads and clears the device error word; maps bits to a status
 int consume_device_error(gca3d_context *ctx, const char *where);
+// the status for an error word already read back (0: GCA3D_OK)
+int device_error_status(gca3d_context *ctx, int word, const char *where);
 
 // ---------------------------------------------------------------------------
 // device helpers

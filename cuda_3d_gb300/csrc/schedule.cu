@@ -56,6 +56,12 @@ struct gca3d_icp_plan
     // the previous one refills h_Tinit only after that copy has run
     cudaEvent_t tinit_copied = nullptr;
     bool tinit_pending = false;
+    // every execute copies the pair states and the device error word back behind the
+    // schedule and records states_ready: results() waits for that copy only, so the
+    // next execute (of this or another plan) may be queued before the results are read
+    cudaEvent_t states_ready = nullptr;
+    bool states_pending = false;
+    int *h_err = nullptr;
 };
 
 namespace
@@ -329,6 +335,10 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
         cudaGraphExecDestroy(pl->exec);
     if (pl->tinit_copied)
         cudaEventDestroy(pl->tinit_copied);
+    if (pl->states_ready)
+        cudaEventDestroy(pl->states_ready);
+    if (pl->h_err)
+        cudaFreeHost(pl->h_err);
     if (pl->side)
         cudaStreamDestroy(pl->side);
     if (pl->graph)
@@ -413,6 +423,7 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
         cudaMalloc(&pl->d_state, sizeof(PairState) * P) != cudaSuccess ||
         cudaMalloc(&pl->d_Tinit, sizeof(double) * 16 * P) != cudaSuccess ||
         cudaMallocHost(&pl->h_state, sizeof(PairState) * P) != cudaSuccess ||
+        cudaMallocHost(&pl->h_err, sizeof(int)) != cudaSuccess ||
         cudaMallocHost(&pl->h_Tinit, sizeof(double) * 16 * P) != cudaSuccess)
     {
         cudaGetLastError();
@@ -514,6 +525,14 @@ int gca3d_icp_plan_execute(gca3d_icp_plan *pl, const double *T_init, gca3d_icp_r
     }
     else if ((st = run_with_arena(pl, false)))
         return st;
+    if (!pl->states_ready)
+        GCA_CUDA(ctx, cudaEventCreateWithFlags(&pl->states_ready, cudaEventDisableTiming));
+    GCA_CUDA(ctx, cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(PairState) * pl->P, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    GCA_CUDA(ctx, cudaMemcpyAsync(pl->h_err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GCA_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    GCA_CUDA(ctx, cudaEventRecord(pl->states_ready, ctx->stream));
+    pl->states_pending = true;
     if (!results)
         return GCA3D_OK;
     return gca3d_icp_plan_results(pl, results);
@@ -524,10 +543,11 @@ int gca3d_icp_plan_results(gca3d_icp_plan *pl, gca3d_icp_result *results)
     if (!pl || !results)
         return GCA3D_ERR_INVALID_VALUE;
     gca3d_context *ctx = pl->ctx;
+    if (!pl->states_pending)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: results of a plan never executed");
+    GCA_CUDA(ctx, cudaEventSynchronize(pl->states_ready));
     int st;
-    if ((st = read_states(pl)))
-        return st;
-    if ((st = consume_device_error(ctx, "icp")))
+    if ((st = device_error_status(ctx, *pl->h_err, "icp")))
         return st;
     fill_results(pl, results);
     if (pl->exec)
@@ -543,6 +563,14 @@ int gca3d_icp_plan_results(gca3d_icp_plan *pl, gca3d_icp_result *results)
         pl->kernels_per_run = pl->kernels_static + 3 * loops;
         ctx->launches += pl->kernels_per_run;
     }
+    return GCA3D_OK;
+}
+
+int gca3d_icp_plan_readback_bytes(gca3d_icp_plan *pl, int64_t *bytes)
+{
+    if (!pl || !bytes)
+        return GCA3D_ERR_INVALID_VALUE;
+    *bytes = (int64_t)sizeof(PairState) * pl->P + (int64_t)sizeof(int);
     return GCA3D_OK;
 }
 

@@ -135,6 +135,7 @@ _SIGS = {
     "gca3d_icp_plan_results": [_P, _P],
     "gca3d_icp_plan_destroy": [_P],
     "gca3d_icp_plan_kernels": [_P, C.POINTER(_I64)],
+    "gca3d_icp_plan_readback_bytes": [_P, C.POINTER(_I64)],
     "gca3d_icp_autotune": [_P, C.c_int, _P, _P, C.POINTER(IcpParams), C.c_int, C.POINTER(Tuning),
                            C.POINTER(C.c_double)],
     "gca3d_radius_outlier_removal": [_P, _P, _F, C.c_int, _P],
@@ -410,6 +411,12 @@ class IcpPlan:
     def kernels(self):
         n = C.c_int64()
         self.ctx.check(self.ctx.L.gca3d_icp_plan_kernels(self.h, C.byref(n)))
+        return n.value
+
+    def readback_bytes(self):
+        """bytes an execute copies back to the host"""
+        n = C.c_int64()
+        self.ctx.check(self.ctx.L.gca3d_icp_plan_readback_bytes(self.h, C.byref(n)))
         return n.value
 
     def __del__(self):

@@ -324,10 +324,14 @@ int gca3d_icp_plan_create(gca3d_context *ctx, int n_pairs, gca3d_cloud *const *s
  * which case execute does not synchronise */
 int gca3d_icp_plan_execute(gca3d_icp_plan *plan, const double *T_init,
                            gca3d_icp_result *results);
-/* the results of the plan's last execute: waits for it on the context stream.  With
- * execute(..., NULL) first, the host is free in between, e.g. to enqueue the next
- * step's uploads on another context's stream. */
+/* the results of the plan's last execute: waits for that execute only (its copy of
+ * the pair states, queued behind it), not for work queued after it.  With
+ * execute(..., NULL) first, the host is free in between: it can enqueue the next
+ * step's uploads on another context's stream and the next execute of another plan
+ * (which then runs right behind this one) before reading these results. */
 int gca3d_icp_plan_results(gca3d_icp_plan *plan, gca3d_icp_result *results);
+/* bytes an execute copies back to the host (the pair states and the error word) */
+int gca3d_icp_plan_readback_bytes(gca3d_icp_plan *plan, int64_t *bytes);
 int gca3d_icp_plan_destroy(gca3d_icp_plan *plan);
 /* kernels one execute launches (graph nodes, or the eager launches of the last run) */
 int gca3d_icp_plan_kernels(gca3d_icp_plan *plan, int64_t *n);

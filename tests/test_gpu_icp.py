@@ -241,6 +241,30 @@ def test_autotune_and_every_launch_shape_give_identical_results(ctx, N, synth):
             assert a["iterations"] == b["iterations"]
 
 
+def test_queued_executes_read_their_own_results(ctx, N, synth):
+    """Two plans executed back to back without waiting: each plan's results() waits
+    for its own execute (the state copy queued behind it) and returns that execute's
+    results, equal to a waiting execute's; a plan never executed has no results."""
+    pairs = synth.batch_pairs(8, seed=6, n_min=20_000, n_max=60_000)
+    srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
+    tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
+    prm = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=True)
+    a = N.IcpPlan(ctx, srcs[:4], tgts[:4], prm)
+    b = N.IcpPlan(ctx, srcs[4:], tgts[4:], prm)
+    res = N.IcpResult * 4
+    assert ctx.L.gca3d_icp_plan_results(a.h, res()) == N.ERR_INVALID_VALUE
+    ref_a, ref_b = a.execute(results=True), b.execute(results=True)
+    for _ in range(3):
+        a.execute(results=False)
+        b.execute(results=False)
+        got_a = a.results()
+        got_b = b.results()
+        for ref, got in ((ref_a, got_a), (ref_b, got_b)):
+            for x, y in zip(ref, got):
+                np.testing.assert_array_equal(x["T"], y["T"])
+                assert x["iterations"] == y["iterations"]
+
+
 @pytest.mark.parametrize("use_graph", [True, False])
 @pytest.mark.parametrize("compensated", [True, False])
 def test_fused_and_separate_finalize_agree(ctx, N, synth, use_graph, compensated):
