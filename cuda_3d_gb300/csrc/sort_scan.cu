@@ -239,6 +239,185 @@ __global__ void k_sort_prep(SortCtl *ctl, SortSeg S, const int32_t *seg_off, int
     }
 }
 
+// the lanes of the warp whose value equals this lane's, for values below 512: one
+// ballot per bit, each lane keeping the lanes that agree with it on every bit
+__device__ __forceinline__ unsigned digit_peers(uint32_t d)
+{
+    unsigned m = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 9; ++b)
+    {
+        const bool bit = (d >> b) & 1u;
+        const unsigned v = __ballot_sync(0xffffffffu, bit);
+        m &= bit ? v : ~v;
+    }
+    return m;
+}
+
+// what one tile of a pass works on
+struct TileJob
+{
+    uint32_t tile;
+    int first, seg, seg_b, seg_e, tile_base, cnt, shift, pass;
+    const uint64_t *kin;
+    const int32_t *vin;
+    uint64_t *kout;
+    int32_t *vout;
+    uint32_t *status;
+};
+
+// one tile of a pass: rank, stage in tile order, look back, scatter.  Packed keys carry
+// their index, so that variant holds no value registers.
+template <bool Packed>
+__device__ __forceinline__ void sort_tile(const TileJob &J, SortCtl *ctl, const SortSeg &S, int *d_err,
+                                          uint32_t (*s_whist)[256], uint32_t *s_excl, uint32_t *s_gbase,
+                                          uint64_t *s_keys, int32_t *s_vals, uint32_t *s_wsum)
+{
+    const uint32_t tile = J.tile;
+    const int first = J.first, seg = J.seg, seg_b = J.seg_b, seg_e = J.seg_e, tile_base = J.tile_base, cnt = J.cnt;
+    const int shift = J.shift, pass = J.pass;
+    const uint64_t *kin = J.kin;
+    const int32_t *vin = J.vin;
+    uint64_t *kout = J.kout;
+    int32_t *vout = J.vout;
+    uint32_t *status = J.status;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+
+    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads)
+        (&s_whist[0][0])[i] = 0;
+    __syncthreads();
+
+    uint64_t k[kSortItems];
+    int32_t v[kSortItems];
+    uint32_t rank[kSortItems];
+    uint32_t dig4[kSortItems / 4] = {}; // the digits, four per word
+    const int base = warp * 32 * kSortItems; // within the tile
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        const int idx = base + it * 32 + lane;
+        k[it] = idx < cnt ? kin[tile_base + idx] : 0;
+        v[it] = idx < cnt && !Packed ? vin[tile_base + idx] : 0;
+        dig4[it / 4] |= ((uint32_t)(k[it] >> shift) & 255u) << (8 * (it % 4));
+    }
+    // warp-level stable ranking: the lanes holding the same digit (one ballot per digit
+    // bit, a fixed cost, where a match instruction costs more the more distinct digits
+    // the warp holds) read the warp's count of that digit, and the lowest of them adds
+    // their number to it
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        const bool in = base + it * 32 + lane < cnt;
+        const uint32_t d = (dig4[it / 4] >> (8 * (it % 4))) & 255u;
+        const unsigned peers = digit_peers(in ? d : 256u);
+        const uint32_t b = s_whist[warp][d];
+        __syncwarp();
+        if (in && (peers & lt_mask) == 0u)
+            s_whist[warp][d] = b + __popc(peers);
+        rank[it] = b + __popc(peers & lt_mask);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: prefix over warps, tile total
+    const int t = threadIdx.x;
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w)
+    {
+        uint32_t c = s_whist[w][t];
+        s_whist[w][t] = tot;
+        tot += c;
+    }
+    // this tile's count of digit t, published for the segment's tiles after it
+    uint32_t *st = status + (int64_t)tile * 256 + t;
+    st_release(st, (tile == first ? kFlagInc : kFlagAgg) | tot);
+    // exclusive scan of the tile totals over digits (block scan of 256 values)
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_wsum[warp] = x;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int w = 0; w < warp; ++w)
+        wpre += s_wsum[w];
+    const uint32_t tile_excl = wpre + x - tot;
+    s_excl[t] = tile_excl;
+    __syncthreads();
+    // stage in tile-sorted order (needs only this tile's counts), so the keys leave
+    // the registers before the look-back
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+    {
+        if (base + it * 32 + lane < cnt)
+        {
+            const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
+            const uint32_t pl = s_excl[d] + s_whist[warp][d] + rank[it];
+            s_keys[pl] = k[it];
+            if (!Packed)
+                s_vals[pl] = v[it];
+        }
+    }
+    // decoupled look-back across the segment's earlier tiles for digit t
+    uint32_t excl = 0;
+    if ((int)tile > first)
+    {
+        // the predecessors' states for this digit, kLookWindow at a time (independent
+        // relaxed loads), consumed nearest first up to the nearest inclusive one (the
+        // segment's first tile publishes an inclusive state at once)
+        bool found = false;
+        const uint32_t limit = wait_limit(d_err);
+        for (int64_t p = (int64_t)tile - 1; p >= first && !found; p -= kLookWindow)
+        {
+            uint32_t s[kLookWindow];
+#pragma unroll
+            for (int j = 0; j < kLookWindow; ++j)
+                s[j] = p - j >= first ? ld_relaxed(status + (p - j) * 256 + t) : kFlagInc;
+#pragma unroll
+            for (int j = 0; j < kLookWindow; ++j)
+            {
+                if (found)
+                    break;
+                uint32_t spins = 0;
+                while ((s[j] & kFlagMask) == 0)
+                {
+                    if (++spins > limit)
+                    {
+                        atomicOr(d_err, kErrTimeout);
+                        break;
+                    }
+                    if (spins > 64)
+                        __nanosleep(64);
+                    s[j] = ld_relaxed(status + (p - j) * 256 + t);
+                }
+                excl += s[j] & kCountMask;
+                if ((s[j] & kFlagMask) != kFlagAgg)
+                    found = true;
+            }
+        }
+        st_release(st, kFlagInc | (excl + tot));
+    }
+    s_gbase[t] = S.doff[((size_t)seg * 8 + pass) * 256 + t] + excl - tile_excl;
+    __syncthreads();
+    for (int j = threadIdx.x; j < cnt; j += kSortThreads)
+    {
+        uint64_t kk = s_keys[j];
+        uint32_t d = (uint32_t)(kk >> shift) & 255u;
+        uint32_t g = s_gbase[d] + j;
+        if (!GCA_INDEX_OK((int)g - seg_b, seg_e - seg_b, d_err))
+            continue;
+        kout[g] = kk;
+        if (!Packed)
+            vout[g] = s_vals[j];
+    }
+}
+
 __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     uint64_t *keys0, int32_t *vals0, uint64_t *keys1, int32_t *vals1, SortCtl *ctl, SortSeg S,
     const int32_t *seg_off, int P, uint32_t *status_base, int64_t status_words, int pass, const int *d_ib,
@@ -294,150 +473,12 @@ __global__ void __launch_bounds__(kSortThreads, 4) k_sort_pass(
     uint64_t *kout = sel ? keys0 : keys1;
     int32_t *vout = sel ? vals0 : vals1;
     // a non-trivial pass lies below bit 64 (the digits above are zero, so trivial)
-    const bool packed = *d_ib != 0;
     const int shift = *d_kshift + pass * 8;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned lt_mask = (1u << lane) - 1u;
-
-    for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads)
-        (&s_whist[0][0])[i] = 0;
-    __syncthreads();
-
-    uint64_t k[kSortItems];
-    int32_t v[kSortItems];
-    uint32_t dig[kSortItems], rank[kSortItems];
-    const int base = warp * 32 * kSortItems; // within the tile
-#pragma unroll
-    for (int it = 0; it < kSortItems; ++it)
-    {
-        const int idx = base + it * 32 + lane;
-        if (idx < cnt)
-        {
-            k[it] = kin[tile_base + idx];
-            v[it] = packed ? 0 : vin[tile_base + idx];
-            dig[it] = (uint32_t)(k[it] >> shift) & 255u;
-        }
-        else
-        {
-            k[it] = 0;
-            v[it] = 0;
-            dig[it] = 256u;
-        }
-    }
-    // warp-level stable ranking (match peers with the same digit)
-#pragma unroll
-    for (int it = 0; it < kSortItems; ++it)
-    {
-        unsigned peers = __match_any_sync(0xffffffffu, dig[it]);
-        int leader = __ffs(peers) - 1;
-        uint32_t b = 0;
-        if (lane == leader && dig[it] < 256u)
-        {
-            b = s_whist[warp][dig[it]];
-            s_whist[warp][dig[it]] = b + __popc(peers);
-        }
-        b = __shfl_sync(0xffffffffu, b, leader);
-        rank[it] = b + __popc(peers & lt_mask);
-        __syncwarp();
-    }
-    __syncthreads();
-    // per digit: prefix over warps, tile total
-    const int t = threadIdx.x;
-    uint32_t tot = 0;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; ++w)
-    {
-        uint32_t c = s_whist[w][t];
-        s_whist[w][t] = tot;
-        tot += c;
-    }
-    // this tile's count of digit t, published for the segment's tiles after it
-    uint32_t *st = status + (int64_t)tile * 256 + t;
-    st_release(st, (tile == first ? kFlagInc : kFlagAgg) | tot);
-    // exclusive scan of the tile totals over digits (block scan of 256 values)
-    uint32_t x = tot;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o)
-            x += y;
-    }
-    if (lane == 31)
-        s_wsum[warp] = x;
-    __syncthreads();
-    uint32_t wpre = 0;
-    for (int w = 0; w < warp; ++w)
-        wpre += s_wsum[w];
-    const uint32_t tile_excl = wpre + x - tot;
-    s_excl[t] = tile_excl;
-    __syncthreads();
-    // stage in tile-sorted order (needs only this tile's counts), so the keys leave
-    // the registers before the look-back
-#pragma unroll
-    for (int it = 0; it < kSortItems; ++it)
-    {
-        if (base + it * 32 + lane < cnt)
-        {
-            const uint32_t d = (uint32_t)(k[it] >> shift) & 255u;
-            const uint32_t pl = s_excl[d] + s_whist[warp][d] + rank[it];
-            s_keys[pl] = k[it];
-            if (!packed)
-                s_vals[pl] = v[it];
-        }
-    }
-    // decoupled look-back across the segment's earlier tiles for digit t
-    uint32_t excl = 0;
-    if ((int)tile > first)
-    {
-        // the predecessors' states for this digit, kLookWindow at a time (independent
-        // relaxed loads), consumed nearest first up to the nearest inclusive one (the
-        // segment's first tile publishes an inclusive state at once)
-        bool found = false;
-        const uint32_t limit = wait_limit(d_err);
-        for (int64_t p = (int64_t)tile - 1; p >= first && !found; p -= kLookWindow)
-        {
-            uint32_t s[kLookWindow];
-#pragma unroll
-            for (int j = 0; j < kLookWindow; ++j)
-                s[j] = p - j >= first ? ld_relaxed(status + (p - j) * 256 + t) : kFlagInc;
-#pragma unroll
-            for (int j = 0; j < kLookWindow; ++j)
-            {
-                if (found)
-                    break;
-                uint32_t spins = 0;
-                while ((s[j] & kFlagMask) == 0)
-                {
-                    if (++spins > limit)
-                    {
-                        atomicOr(d_err, kErrTimeout);
-                        break;
-                    }
-                    if (spins > 64)
-                        __nanosleep(64);
-                    s[j] = ld_relaxed(status + (p - j) * 256 + t);
-                }
-                excl += s[j] & kCountMask;
-                if ((s[j] & kFlagMask) != kFlagAgg)
-                    found = true;
-            }
-        }
-        st_release(st, kFlagInc | (excl + tot));
-    }
-    s_gbase[t] = S.doff[((size_t)seg * 8 + pass) * 256 + t] + excl - tile_excl;
-    __syncthreads();
-    for (int j = threadIdx.x; j < cnt; j += kSortThreads)
-    {
-        uint64_t kk = s_keys[j];
-        uint32_t d = (uint32_t)(kk >> shift) & 255u;
-        uint32_t g = s_gbase[d] + j;
-        if (!GCA_INDEX_OK((int)g - seg_b, seg_e - seg_b, d_err))
-            continue;
-        kout[g] = kk;
-        if (!packed)
-            vout[g] = s_vals[j];
-    }
+    const TileJob J{tile, first, seg, seg_b, seg_e, tile_base, cnt, shift, pass, kin, vin, kout, vout, status};
+    if (*d_ib != 0)
+        sort_tile<true>(J, ctl, S, d_err, s_whist, s_excl, s_gbase, s_keys, s_vals, s_wsum);
+    else
+        sort_tile<false>(J, ctl, S, d_err, s_whist, s_excl, s_gbase, s_keys, s_vals, s_wsum);
 }
 
 int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *seg_off, int P, int64_t cap, int64_t max_seg_cap,
