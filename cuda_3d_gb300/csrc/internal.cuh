@@ -438,5 +438,10 @@ int radix_sort(gca3d_context *ctx, SortBuffers &sb, const int32_t *seg_off, int 
 // exclusive scan of int32 values (n on the device), writes total to *d_total
 int exclusive_scan(gca3d_context *ctx, const int32_t *in, int32_t *out, const int32_t *d_n,
                    int64_t cap, int32_t *d_total);
+// the runs of equal keys of a sorted view in one scan: starts[r] the first position of
+// run r, starts[runs] = n, *d_runs the number of runs, seg_first[s] the first run of
+// segment s (left untouched, e.g. -1, for an empty segment)
+int run_scan(gca3d_context *ctx, const SortBuffers &sb, const int32_t *d_n, int64_t cap, const KeyLayout *lay,
+             int32_t *starts, int32_t *seg_first, int32_t *d_runs);
 
 } // namespace gca3d

@@ -543,11 +543,65 @@ struct ScanCtl
     uint32_t tile_ctr;
 };
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict__ in, int32_t *out,
-                                                       const int32_t *d_n, ScanCtl *ctl,
-                                                       unsigned long long *status, int32_t *d_total,
-                                                       int *d_err)
+// what a scan reads and writes: item(i) is the value at i < n, put(i, e, v) receives
+// the exclusive prefix e of item i (value v), total(t, n) the sum of all n items;
+// bind() makes the copy a thread uses (device-side state read once)
+struct ArrayScan
 {
+    const int32_t *in;
+    int32_t *out;
+    int32_t *d_total;
+    __device__ ArrayScan bind() const { return *this; }
+    __device__ int item(int64_t i) const { return in[i]; }
+    __device__ void put(int64_t i, long long e, int) const { out[i] = (int32_t)e; }
+    __device__ void total(long long t, int) const
+    {
+        if (d_total)
+            *d_total = (int32_t)t;
+    }
+};
+
+// the runs of equal keys in a sorted view: item(i) is 1 where a run starts, and a run's
+// exclusive prefix is its index, so put() writes the run starts (starts[run] = i,
+// starts[runs] = n) and each segment's first run (seg_first, preset to -1)
+struct RunScan
+{
+    SortBuffers sb;
+    const KeyLayout *lay;
+    int32_t *starts;
+    int32_t *seg_first;
+    int32_t *d_runs;
+    SortedView sv; // set by bind(): the buffer and key shift the sort left
+    __device__ RunScan bind() const
+    {
+        RunScan r = *this;
+        r.sv = sorted_view(sb);
+        return r;
+    }
+    __device__ int item(int64_t i) const { return i == 0 || sv.key((int)i) != sv.key((int)i - 1) ? 1 : 0; }
+    __device__ void put(int64_t i, long long e, int v) const
+    {
+        if (!v)
+            return;
+        starts[e] = (int32_t)i;
+        const KeyLayout L = *lay;
+        const int segshift = L.bx + L.by + L.bz;
+        const int seg = L.bseg ? (int)(sv.key((int)i) >> segshift) : 0;
+        if (i == 0 || (L.bseg && (int)(sv.key((int)i - 1) >> segshift) != seg))
+            seg_first[seg] = (int32_t)e;
+    }
+    __device__ void total(long long t, int n) const
+    {
+        *d_runs = (int32_t)t;
+        starts[t] = n;
+    }
+};
+
+template <class Op>
+__global__ void __launch_bounds__(kScanThreads) k_scan(const Op op_in, const int32_t *d_n, ScanCtl *ctl,
+                                                       unsigned long long *status, int *d_err)
+{
+    const Op op = op_in.bind();
     __shared__ uint32_t s_tile;
     __shared__ long long s_wsum[kScanThreads / 32];
     __shared__ long long s_prefix;
@@ -559,8 +613,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict
     const int tile = (int)s_tile;
     if (tile >= ntiles)
     {
-        if (tile == 0 && threadIdx.x == 0 && d_total)
-            *d_total = 0; // empty input
+        if (tile == 0 && threadIdx.x == 0)
+            op.total(0, 0); // empty input
         return;
     }
     const int64_t base = (int64_t)tile * kScanTile + threadIdx.x * kScanItems;
@@ -569,7 +623,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i)
     {
-        v[i] = base + i < n ? (long long)in[base + i] : 0;
+        v[i] = base + i < n ? (long long)op.item(base + i) : 0;
         tsum += v[i];
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -636,8 +690,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict
         if (lane == 0)
         {
             s_prefix = excl;
-            if (tile == ntiles - 1 && d_total)
-                *d_total = (int32_t)(excl + agg);
+            if (tile == ntiles - 1)
+                op.total(excl + agg, n);
         }
     }
     __syncthreads();
@@ -649,7 +703,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const int32_t *__restrict
     for (int i = 0; i < kScanItems; ++i)
     {
         if (base + i < n)
-            out[base + i] = (int32_t)run;
+            op.put(base + i, run, (int)v[i]);
         run += v[i];
     }
 }
@@ -664,8 +718,24 @@ int exclusive_scan(gca3d_context *ctx, const int32_t *in, int32_t *out, const in
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "exclusive_scan: scratch");
     GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(ScanCtl), ctx->stream));
     GCA_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(unsigned long long) * (ntiles > 0 ? ntiles : 1), ctx->stream));
-    k_scan<<<(int)(ntiles > 0 ? ntiles : 1), kScanThreads, 0, ctx->stream>>>(in, out, d_n, ctl, status, d_total,
-                                                                             ctx->d_err);
+    k_scan<<<(int)(ntiles > 0 ? ntiles : 1), kScanThreads, 0, ctx->stream>>>(ArrayScan{in, out, d_total}, d_n, ctl,
+                                                                             status, ctx->d_err);
+    GCA_CHECK_LAUNCH(ctx);
+    return GCA3D_OK;
+}
+
+int run_scan(gca3d_context *ctx, const SortBuffers &sb, const int32_t *d_n, int64_t cap, const KeyLayout *lay,
+             int32_t *starts, int32_t *seg_first, int32_t *d_runs)
+{
+    const int64_t ntiles = (cap + kScanTile - 1) / kScanTile;
+    ScanCtl *ctl = ctx->arena.get<ScanCtl>(1);
+    unsigned long long *status = ctx->arena.get<unsigned long long>(ntiles > 0 ? ntiles : 1);
+    if (!ctl || !status)
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "run_scan: scratch");
+    GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(ScanCtl), ctx->stream));
+    GCA_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(unsigned long long) * (ntiles > 0 ? ntiles : 1), ctx->stream));
+    k_scan<<<(int)(ntiles > 0 ? ntiles : 1), kScanThreads, 0, ctx->stream>>>(
+        RunScan{sb, lay, starts, seg_first, d_runs, SortedView{}}, d_n, ctl, status, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
@@ -711,7 +781,7 @@ int gca3d_selfcheck_wait(gca3d_context *ctx, int tiles, int polls, int *wait_sta
     GCA_CUDA(ctx, cudaEventCreate(&e0));
     GCA_CUDA(ctx, cudaEventCreate(&e1));
     cudaEventRecord(e0, ctx->stream);
-    k_scan<<<tiles - 1, kScanThreads, 0, ctx->stream>>>(in, out, d_n, ctl, status, nullptr, ctx->d_err);
+    k_scan<<<tiles - 1, kScanThreads, 0, ctx->stream>>>(ArrayScan{in, out, nullptr}, d_n, ctl, status, ctx->d_err);
     const cudaError_t le = cudaGetLastError();
     ctx->launches++;
     cudaEventRecord(e1, ctx->stream);

@@ -205,35 +205,6 @@ __global__ void k_voxel_keys(const SegSrc *src, const int32_t *off, const float3
     }
 }
 
-__global__ void k_run_flags(SortBuffers sb, const int32_t *d_n, int32_t *flags)
-{
-    const SortedView sv = sorted_view(sb);
-    const int n = *d_n;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        flags[i] = (i == 0 || sv.key(i) != sv.key(i - 1)) ? 1 : 0;
-}
-
-// run starts of the sorted keys, and the first run (voxel) of every segment
-__global__ void k_run_starts(const int32_t *flags, const int32_t *vid, const int32_t *d_n, const int32_t *d_m,
-                             int32_t *starts, SortBuffers sb, const KeyLayout *lay, int32_t *seg_first)
-{
-    const int n = *d_n;
-    const SortedView sv = sorted_view(sb);
-    const KeyLayout L = *lay;
-    const int segshift = L.bx + L.by + L.bz;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    {
-        if (!flags[i])
-            continue;
-        starts[vid[i]] = i;
-        const int seg = L.bseg ? (int)(sv.key(i) >> segshift) : 0;
-        if (i == 0 || (L.bseg && (int)(sv.key(i - 1) >> segshift) != seg))
-            seg_first[seg] = vid[i];
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        starts[*d_m] = n;
-}
-
 // segment offsets of the output; empty segments start where the next one does
 __global__ void k_seg_first_to_offsets(const int32_t *seg_first, int P, const int32_t *d_m, int32_t *off)
 {
@@ -318,6 +289,28 @@ __global__ void k_voxel_refine(SortBuffers sb, const int32_t *starts, const int3
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < m; v += gridDim.x * blockDim.x)
     {
         const int s = starts[v], e = starts[v + 1];
+        if (e - s < 256)
+        {
+            // a run of fewer than 256 keys: the eight sub-cell counts are the bytes of one
+            // register, and one multiplication by 0x0101..01 gives their running sums
+            // (byte b of the product: the keys of sub-cells 0..b; shifted one byte up: the
+            // keys of the sub-cells below b), all below 256, so no byte carries
+            uint64_t c = 0;
+            for (int j = s; j < e; ++j)
+                c += 1ull << (8 * (int)((kin[j] >> ks) & 7));
+            uint64_t at = (c * 0x0101010101010101ull) << 8;
+            for (int j = s; j < e; ++j)
+            {
+                const uint64_t w = kin[j];
+                const int sh = 8 * (int)((w >> ks) & 7);
+                const int o = s + (int)((at >> sh) & 255u);
+                at += 1ull << sh;
+                kout[o] = w;
+                if (!packed)
+                    vout[o] = vin[j];
+            }
+            continue;
+        }
         int off[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int j = s; j < e; ++j)
             ++off[(kin[j] >> ks) & 7];
@@ -348,22 +341,16 @@ static int voxel_reduce_stage(gca3d_context *ctx, const SegSrc *d_src, int P, in
 {
     Arena &A = ctx->arena;
     const int64_t cap = std::max<int64_t>(total_cap, 1);
-    int32_t *flags = A.get<int32_t>(cap);
-    int32_t *vid = A.get<int32_t>(cap);
     int32_t *seg_count = A.get<int32_t>(P);
-    if (!flags || !vid || !seg_count)
+    if (!seg_count)
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "voxel_stage: scratch");
     cudaStream_t s = ctx->stream;
     const int32_t *d_n = in_off + P;
     const int gs = std::min(grid_for(total_cap), ctx->num_sms * 8);
-    k_run_flags<<<gs, kBlock, 0, s>>>(sb, d_n, flags);
-    GCA_CHECK_LAUNCH(ctx);
-    int st = exclusive_scan(ctx, flags, vid, d_n, total_cap, d_m);
+    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0xFF, sizeof(int32_t) * P, s));
+    int st = run_scan(ctx, sb, d_n, cap, lay, starts, seg_count, d_m);
     if (st)
         return st;
-    GCA_CUDA(ctx, cudaMemsetAsync(seg_count, 0xFF, sizeof(int32_t) * P, s));
-    k_run_starts<<<gs, kBlock, 0, s>>>(flags, vid, d_n, d_m, starts, sb, lay, seg_count);
-    GCA_CHECK_LAUNCH(ctx);
     GCA_PROF_BEGIN(ctx, kKidVoxelReduce);
     k_voxel_reduce<<<gs, kBlock, 0, s>>>(d_src, in_off, sb, starts, d_m, lay, out.pos, out.col, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
