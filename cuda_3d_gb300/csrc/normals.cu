@@ -351,6 +351,52 @@ __device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, 
         O.nrm_out[gi] = make_float4(n.x, n.y, n.z, 0.0f);
 }
 
+// the sums of one point's walk: first and second moments of the neighbours inside the
+// normal radius (k of them), and the gradient moments G, m inside the gradient radius
+// (gk of them), all about the point
+struct PointMoments
+{
+    float s1x, s1y, s1z, sxx, sxy, sxz, syy, syz, szz;
+    float gxx, gxy, gxz, gyy, gyz, gzz, mx, my, mz;
+    int k, gk;
+};
+
+// what follows a point's walk: the FP32 eigen-solve (or the queue for the FP64 pass),
+// the orientation, the gradient and the stores.  Compiled once and called by every
+// instantiation of the walk, so that the results round alike whichever walk summed
+// the moments.
+__device__ __noinline__ void finish_point(const int32_t *sidx, NormalOut O, int s, float Ip, PointMoments M, bool grad)
+{
+    float3 nrm = make_float3(0.0f, 0.0f, 0.0f);
+    if (M.k >= 3)
+    {
+        const float ik = 1.0f / (float)M.k;
+        const float ux = M.s1x * ik, uy = M.s1y * ik, uz = M.s1z * ik;
+        if (!smallest_eigvec_f32(M.sxx * ik - ux * ux, M.sxy * ik - ux * uy, M.sxz * ik - ux * uz,
+                                 M.syy * ik - uy * uy, M.syz * ik - uy * uz, M.szz * ik - uz * uz, nrm))
+        {
+            const int slot = atomicAdd(O.degen_count, 1);
+            O.degen_list[slot] = s;
+            if (grad)
+            {
+                O.degen_mom[3 * slot] = make_float4(M.gxx, M.gxy, M.gxz, M.gyy);
+                O.degen_mom[3 * slot + 1] = make_float4(M.gyz, M.gzz, M.mx, M.my);
+                O.degen_mom[3 * slot + 2] = make_float4(M.mz, __int_as_float(M.gk), 0.0f, 0.0f);
+            }
+            return; // written by the FP64 pass
+        }
+        // orient against (0, 0, -1) (cuda_estimate_normals.cu:131-151)
+        if (nrm.z > 0.0f)
+            nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+    }
+    const int gi = sidx[s];
+    store_normal(O, s, gi, nrm, Ip);
+    if (grad)
+        store_gradient(O, s, gi,
+                       gradient_from_moments(M.gxx, M.gxy, M.gxz, M.gyy, M.gyz, M.gzz, make_float3(M.mx, M.my, M.mz),
+                                             M.gk, nrm));
+}
+
 // pass 1: PCA normal per grid point in FP32 -- moments about the query point,
 // closed-form eigen-system; points whose smallest eigenvalue is not separated by
 // 1e-3 of the spread are queued for the FP64 pass.  With Grad the same walk sums
@@ -361,7 +407,7 @@ __device__ __forceinline__ void store_normal(const NormalOut &O, int s, int gi, 
 // batches)
 constexpr int kNormScanBatch = 1;
 
-template <bool Grad>
+template <bool Grad, bool SameR>
 __global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *d_n, float rn, int max_nn, NormalOut O)
 {
     const int n = *d_n;
@@ -380,11 +426,13 @@ __global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *
         float s1x = 0, s1y = 0, s1z = 0, sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0;
         float gxx = 0, gxy = 0, gxz = 0, gyy = 0, gyz = 0, gzz = 0, mx = 0, my = 0, mz = 0;
         int k = 0, gk = 0;
+        // the products are added by fused multiply-adds, written out so that every
+        // instantiation rounds the sums alike
         auto acc = [&](float4 q) {
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             s1x += dx, s1y += dy, s1z += dz;
-            sxx += dx * dx, sxy += dx * dy, sxz += dx * dz;
-            syy += dy * dy, syz += dy * dz, szz += dz * dz;
+            sxx = fmaf(dx, dx, sxx), sxy = fmaf(dx, dy, sxy), sxz = fmaf(dx, dz, sxz);
+            syy = fmaf(dy, dy, syy), syz = fmaf(dy, dz, syz), szz = fmaf(dz, dz, szz);
             ++k;
         };
         // every neighbour inside the radius; only when there are more than max_nn
@@ -394,17 +442,31 @@ __global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *
             grid_scan<kNormScanBatch>(g, R, [&](int t, float4 q) {
                 const float d2 = dist2_ref(q.x, q.y, q.z, p.x, p.y, p.z);
                 if (d2 < rn2)
+                {
                     acc(q);
-                if (Grad && d2 < O.grad_r2)
+                    if (SameR)
+                    {
+                        // equal radii: G is the second-moment sum just taken, only m is new
+                        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                        const float dI = g.sint[t] - Ip;
+                        mx = fmaf(dx, dI, mx), my = fmaf(dy, dI, my), mz = fmaf(dz, dI, mz);
+                    }
+                }
+                if (Grad && !SameR && d2 < O.grad_r2)
                 {
                     const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
                     const float dI = g.sint[t] - Ip;
-                    gxx += dx * dx, gxy += dx * dy, gxz += dx * dz;
-                    gyy += dy * dy, gyz += dy * dz, gzz += dz * dz;
-                    mx += dx * dI, my += dy * dI, mz += dz * dI;
+                    gxx = fmaf(dx, dx, gxx), gxy = fmaf(dx, dy, gxy), gxz = fmaf(dx, dz, gxz);
+                    gyy = fmaf(dy, dy, gyy), gyz = fmaf(dy, dz, gyz), gzz = fmaf(dz, dz, gzz);
+                    mx = fmaf(dx, dI, mx), my = fmaf(dy, dI, my), mz = fmaf(dz, dI, mz);
                     ++gk;
                 }
             });
+        if (SameR)
+        {
+            gxx = sxx, gxy = sxy, gxz = sxz, gyy = syy, gyz = syz, gzz = szz;
+            gk = k;
+        }
         if (inside && max_nn > 0 && k > max_nn)
         {
             s1x = s1y = s1z = sxx = sxy = sxz = syy = syz = szz = 0.0f;
@@ -413,33 +475,10 @@ __global__ void __launch_bounds__(256, 4) k_normals32(GridDev g, const int32_t *
             for (int j = 0; j < cnt; ++j)
                 acc(g.spos[list[j].t]);
         }
-        float3 nrm = make_float3(0.0f, 0.0f, 0.0f);
-        if (k >= 3)
-        {
-            const float ik = 1.0f / (float)k;
-            const float ux = s1x * ik, uy = s1y * ik, uz = s1z * ik;
-            if (!smallest_eigvec_f32(sxx * ik - ux * ux, sxy * ik - ux * uy, sxz * ik - ux * uz, syy * ik - uy * uy,
-                                     syz * ik - uy * uz, szz * ik - uz * uz, nrm))
-            {
-                const int slot = atomicAdd(O.degen_count, 1);
-                O.degen_list[slot] = s;
-                if (Grad)
-                {
-                    O.degen_mom[3 * slot] = make_float4(gxx, gxy, gxz, gyy);
-                    O.degen_mom[3 * slot + 1] = make_float4(gyz, gzz, mx, my);
-                    O.degen_mom[3 * slot + 2] = make_float4(mz, __int_as_float(gk), 0.0f, 0.0f);
-                }
-                continue; // written by the FP64 pass
-            }
-            // orient against (0, 0, -1) (cuda_estimate_normals.cu:131-151)
-            if (nrm.z > 0.0f)
-                nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
-        }
-        const int gi = g.sidx[s];
-        store_normal(O, s, gi, nrm, Ip);
-        if (Grad)
-            store_gradient(O, s, gi,
-                           gradient_from_moments(gxx, gxy, gxz, gyy, gyz, gzz, make_float3(mx, my, mz), gk, nrm));
+        finish_point(g.sidx, O, s, Ip,
+                     PointMoments{s1x, s1y, s1z, sxx, sxy, sxz, syy, syz, szz, gxx, gxy, gxz, gyy, gyz, gzz, mx,
+                                  my, mz, k, gk},
+                     Grad);
     }
 }
 
@@ -734,10 +773,13 @@ int normals_stage(gca3d_context *ctx, const Batch &b, const Grid &g, bool do_nor
         if (!O.degen_count || !O.degen_list || (do_grad && !O.degen_mom))
             return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "normals: scratch");
         GCA_CUDA(ctx, cudaMemsetAsync(O.degen_count, 0, sizeof(int), ctx->stream));
-        if (do_grad)
-            k_normals32<true><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
+        // equal radii (the usual case): the gradient's second moments are the normal's
+        if (do_grad && O.grad_r2 == normal_radius * normal_radius)
+            k_normals32<true, true><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
+        else if (do_grad)
+            k_normals32<true, false><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
         else
-            k_normals32<false><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
+            k_normals32<false, false><<<gs, 256, 0, ctx->stream>>>(g.dev, d_n, normal_radius, max_nn, O);
         GCA_CHECK_LAUNCH(ctx);
         // one warp per queued point and a long dependent FP64 chain per point: as many
         // resident blocks as the registers allow, to overlap the chains
