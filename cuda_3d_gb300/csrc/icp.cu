@@ -201,26 +201,85 @@ __device__ __forceinline__ int find_pair(const int *bmap, int P, int b)
     return lo;
 }
 
-// per-scale setup: block map, per-pair counts, reset of the per-scale flags
-__global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
-                            int *bmap_nn, int scale, int nn_chunk)
+// exclusive prefix over the block's kIcpThreads threads of two per-thread counts: each
+// thread gets its own prefixes back in a and b, and every thread the two totals
+__device__ __forceinline__ void block_prefix2(int &a, int &b, int &ta, int &tb)
 {
-    if (threadIdx.x != 0)
-        return;
+    __shared__ int s_a[kIcpThreads], s_b[kIcpThreads];
+    __shared__ int s_ta, s_tb;
+    s_a[threadIdx.x] = a;
+    s_b[threadIdx.x] = b;
+    __syncthreads();
+    if (threadIdx.x < 32)
+    {
+        // 8 per lane, then across the warp
+        constexpr int kPer = kIcpThreads / 32;
+        const int l = threadIdx.x;
+        int va[kPer], vb[kPer], sa = 0, sb = 0;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+        {
+            va[k] = s_a[l * kPer + k];
+            vb[k] = s_b[l * kPer + k];
+            sa += va[k];
+            sb += vb[k];
+        }
+        int ia = sa, ib = sb;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int ya = __shfl_up_sync(0xffffffffu, ia, o), yb = __shfl_up_sync(0xffffffffu, ib, o);
+            if (l >= o)
+                ia += ya, ib += yb;
+        }
+        int ra = ia - sa, rb = ib - sb;
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+        {
+            s_a[l * kPer + k] = ra;
+            s_b[l * kPer + k] = rb;
+            ra += va[k];
+            rb += vb[k];
+        }
+        if (l == 31)
+        {
+            s_ta = ra;
+            s_tb = rb;
+        }
+    }
+    __syncthreads();
+    a = s_a[threadIdx.x];
+    b = s_b[threadIdx.x];
+    ta = s_ta;
+    tb = s_tb;
+}
+
+// per-scale setup: block map, per-pair counts, reset of the per-scale flags; the
+// pairs split over the block's threads, the maps by a block prefix
+__global__ void __launch_bounds__(kIcpThreads) k_icp_setup(PairState *st, int P, const int32_t *src_off,
+                                                           const int32_t *tgt_off, int *bmap, int *bmap_nn, int scale,
+                                                           int nn_chunk)
+{
+    __shared__ int s_nact;
+    if (threadIdx.x == 0)
+        s_nact = 0;
+    __syncthreads();
     const int chunk = kIcpChunk;
-    int b = 0, bn = 0;
-    for (int p = 0; p < P; ++p)
+    const int per = (P + kIcpThreads - 1) / kIcpThreads;
+    const int p0 = min(P, (int)threadIdx.x * per), p1 = min(P, p0 + per);
+    int b = 0, bn = 0, na = 0;
+    for (int p = p0; p < p1; ++p)
     {
         PairState &S = st[p];
         const int ns = src_off[p + 1] - src_off[p];
         const int nt = tgt_off[p + 1] - tgt_off[p];
         const int nb = (ns > 0 && nt > 0) ? (ns + chunk - 1) / chunk : 0;
-        bmap[p] = b;
+        const int nbn = (ns > 0 && nt > 0) ? (ns + nn_chunk - 1) / nn_chunk : 0;
         b += nb;
-        bmap_nn[p] = bn;
-        bn += (ns > 0 && nt > 0) ? (ns + nn_chunk - 1) / nn_chunk : 0;
+        bn += nbn;
+        na += nb > 0;
         S.nblocks = nb;
-        S.nblocks_nn = (ns > 0 && nt > 0) ? (ns + nn_chunk - 1) / nn_chunk : 0;
+        S.nblocks_nn = nbn;
         S.nsrc = ns;
         S.ntgt = nt;
         S.ticket = 0;
@@ -243,13 +302,24 @@ __global__ void k_icp_setup(PairState *st, int P, const int32_t *src_off, const 
             S.rmse_ref = S.fitness = S.inlier_rmse = 0.0;
         }
     }
-    int nact = 0;
-    for (int p = 0; p < P; ++p)
-        nact += st[p].active;
-    bmap[P] = b;
-    bmap[P + 1] = nact; // pairs the fused accumulate finalizes this iteration
-    bmap_nn[P] = bn;
-    bmap_nn[P + 1] = 0; // the correspondence kernel's work queue
+    if (na)
+        atomicAdd(&s_nact, na);
+    int tb, tbn;
+    block_prefix2(b, bn, tb, tbn);
+    for (int p = p0; p < p1; ++p)
+    {
+        bmap[p] = b;
+        bmap_nn[p] = bn;
+        b += st[p].nblocks;
+        bn += st[p].nblocks_nn;
+    }
+    if (threadIdx.x == 0)
+    {
+        bmap[P] = tb;
+        bmap[P + 1] = s_nact; // pairs the fused accumulate finalizes this iteration
+        bmap_nn[P] = tbn;
+        bmap_nn[P + 1] = 0; // the correspondence kernel's work queue
+    }
 }
 
 __global__ void k_state_init(PairState *st, int P, const double *T_init)
@@ -571,7 +641,6 @@ __device__ __noinline__ void finalize_pair(PairState *st, int P, int pair, const
 // iteration is finalized.
 __device__ __noinline__ void rebuild_maps(PairState *st, int P, int *bmap, int *bmap_nn, IcpLoop loop)
 {
-    __shared__ int s_sum[kIcpThreads], s_sum_nn[kIcpThreads];
     __shared__ int s_nact;
     if (threadIdx.x == 0)
         s_nact = 0;
@@ -588,56 +657,21 @@ __device__ __noinline__ void rebuild_maps(PairState *st, int P, int *bmap, int *
         }
     if (na)
         atomicAdd(&s_nact, na);
-    s_sum[threadIdx.x] = a;
-    s_sum_nn[threadIdx.x] = an;
-    __syncthreads();
-    if (threadIdx.x < 32)
+    int ta, tn;
+    block_prefix2(a, an, ta, tn);
+    if (threadIdx.x == 0)
     {
-        // exclusive prefix of the 256 per-thread sums: 8 per lane, then across the warp
-        const int l = threadIdx.x;
-        int va[kIcpThreads / 32], vn[kIcpThreads / 32], sa = 0, sn = 0;
-#pragma unroll
-        for (int k = 0; k < kIcpThreads / 32; ++k)
+        bmap[P] = ta;
+        bmap[P + 1] = s_nact;
+        bmap_nn[P] = tn;
+        bmap_nn[P + 1] = 0;
+        *loop.ticket = 0u;
+        if (loop.iter)
         {
-            va[k] = s_sum[l * (kIcpThreads / 32) + k];
-            vn[k] = s_sum_nn[l * (kIcpThreads / 32) + k];
-            sa += va[k];
-            sn += vn[k];
-        }
-        int ia = sa, in = sn;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const int ya = __shfl_up_sync(0xffffffffu, ia, o), yn = __shfl_up_sync(0xffffffffu, in, o);
-            if (l >= o)
-                ia += ya, in += yn;
-        }
-        int ra = ia - sa, rn = in - sn;
-#pragma unroll
-        for (int k = 0; k < kIcpThreads / 32; ++k)
-        {
-            s_sum[l * (kIcpThreads / 32) + k] = ra;
-            s_sum_nn[l * (kIcpThreads / 32) + k] = rn;
-            ra += va[k];
-            rn += vn[k];
-        }
-        if (l == 31)
-        {
-            bmap[P] = ra;
-            bmap[P + 1] = s_nact;
-            bmap_nn[P] = rn;
-            bmap_nn[P + 1] = 0;
-            *loop.ticket = 0u;
-            if (loop.iter)
-            {
-                const int it = ++(*loop.iter);
-                cudaGraphSetConditional(loop.handle, (rn > 0 && it < loop.max_iter) ? 1u : 0u);
-            }
+            const int it = ++(*loop.iter);
+            cudaGraphSetConditional(loop.handle, (tn > 0 && it < loop.max_iter) ? 1u : 0u);
         }
     }
-    __syncthreads();
-    a = s_sum[threadIdx.x];
-    an = s_sum_nn[threadIdx.x];
     for (int q = p0; q < p1; ++q)
     {
         bmap[q] = a;
@@ -791,7 +825,7 @@ IcpShape icp_shape(const gca3d_tuning &t)
 int icp_setup(gca3d_context *ctx, PairState *st, int P, const int32_t *src_off, const int32_t *tgt_off, int *bmap,
               int *bmap_nn, int scale, int nn_chunk)
 {
-    k_icp_setup<<<1, 32, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, bmap_nn, scale, nn_chunk);
+    k_icp_setup<<<1, kIcpThreads, 0, ctx->stream>>>(st, P, src_off, tgt_off, bmap, bmap_nn, scale, nn_chunk);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }

@@ -53,15 +53,11 @@ struct SortSeg
     int32_t *tile_first;
 };
 
-__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v)
+// a status word carries its flag and count together in one aligned 32-bit word, and
+// nothing else is read on the strength of it, so publishing needs no release fence
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v)
 {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
-{
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 // a state word holds its flag and its count together, so a reader that uses only
 // the word itself needs no ordering: relaxed loads, several in flight at once
@@ -331,7 +327,7 @@ __device__ __forceinline__ void sort_tile(const TileJob &J, SortCtl *ctl, const 
     }
     // this tile's count of digit t, published for the segment's tiles after it
     uint32_t *st = status + (int64_t)tile * 256 + t;
-    st_release(st, (tile == first ? kFlagInc : kFlagAgg) | tot);
+    st_relaxed(st, (tile == first ? kFlagInc : kFlagAgg) | tot);
     // exclusive scan of the tile totals over digits (block scan of 256 values)
     uint32_t x = tot;
 #pragma unroll
@@ -401,7 +397,7 @@ __device__ __forceinline__ void sort_tile(const TileJob &J, SortCtl *ctl, const 
                     found = true;
             }
         }
-        st_release(st, kFlagInc | (excl + tot));
+        st_relaxed(st, kFlagInc | (excl + tot));
     }
     s_gbase[t] = S.doff[((size_t)seg * 8 + pass) * 256 + t] + excl - tile_excl;
     __syncthreads();
