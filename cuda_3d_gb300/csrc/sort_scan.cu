@@ -539,9 +539,62 @@ struct ScanCtl
     uint32_t tile_ctr;
 };
 
+// warp 0 of a scan tile (all 32 lanes): publishes the tile's aggregate, looks back over
+// the earlier tiles and publishes the inclusive prefix; returns the tile's exclusive
+// prefix to every lane.  The 32 nearest predecessors' states are read at once (each
+// wait bounded), the nearest inclusive one is found by ballot and the states up to it
+// are summed across the warp; only a window of aggregates moves the look-back 32 tiles
+// further.
+__device__ __forceinline__ long long scan_lookback(int tile, long long agg, unsigned long long *status, int *d_err)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long *st = status + tile;
+    long long excl = 0;
+    if (lane == 0)
+        st_release64(st, (tile == 0 ? kSFlagInc : kSFlagAgg) | (unsigned long long)agg);
+    if (tile > 0)
+    {
+        for (int top = tile - 1;; top -= 32)
+        {
+            const int p = top - lane;
+            unsigned long long s = kSFlagInc; // before tile 0: an inclusive zero
+            if (p >= 0)
+            {
+                const uint32_t limit = wait_limit(d_err);
+                uint32_t spins = 0;
+                s = ld_acquire64(status + p);
+                while ((s & kSFlagMask) == 0)
+                {
+                    if (++spins > limit)
+                    {
+                        atomicOr(d_err, kErrTimeout);
+                        break;
+                    }
+                    if (spins > 64)
+                        __nanosleep(64);
+                    s = ld_acquire64(status + p);
+                }
+            }
+            const unsigned inc = __ballot_sync(0xffffffffu, (s & kSFlagMask) != kSFlagAgg);
+            const int stop = inc ? __ffs(inc) - 1 : 31;
+            long long v = lane <= stop ? (long long)(s & kSValMask) : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+            excl += v;
+            if (inc)
+                break;
+        }
+        if (lane == 0)
+            st_release64(st, kSFlagInc | (unsigned long long)(excl + agg));
+    }
+    return excl;
+}
+
 // what a scan reads and writes: item(i) is the value at i < n, put(i, e, v) receives
 // the exclusive prefix e of item i (value v), total(t, n) the sum of all n items;
 // bind() makes the copy a thread uses (device-side state read once)
+
 struct ArrayScan
 {
     const int32_t *in;
@@ -554,42 +607,6 @@ struct ArrayScan
     {
         if (d_total)
             *d_total = (int32_t)t;
-    }
-};
-
-// the runs of equal keys in a sorted view: item(i) is 1 where a run starts, and a run's
-// exclusive prefix is its index, so put() writes the run starts (starts[run] = i,
-// starts[runs] = n) and each segment's first run (seg_first, preset to -1)
-struct RunScan
-{
-    SortBuffers sb;
-    const KeyLayout *lay;
-    int32_t *starts;
-    int32_t *seg_first;
-    int32_t *d_runs;
-    SortedView sv; // set by bind(): the buffer and key shift the sort left
-    __device__ RunScan bind() const
-    {
-        RunScan r = *this;
-        r.sv = sorted_view(sb);
-        return r;
-    }
-    __device__ int item(int64_t i) const { return i == 0 || sv.key((int)i) != sv.key((int)i - 1) ? 1 : 0; }
-    __device__ void put(int64_t i, long long e, int v) const
-    {
-        if (!v)
-            return;
-        starts[e] = (int32_t)i;
-        const KeyLayout L = *lay;
-        const int segshift = L.bx + L.by + L.bz;
-        const int seg = L.bseg ? (int)(sv.key((int)i) >> segshift) : 0;
-        if (i == 0 || (L.bseg && (int)(sv.key((int)i - 1) >> segshift) != seg))
-            seg_first[seg] = (int32_t)e;
-    }
-    __device__ void total(long long t, int n) const
-    {
-        *d_runs = (int32_t)t;
-        starts[t] = n;
     }
 };
 
@@ -634,55 +651,12 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const Op op_in, const int
     if (lane == 31)
         s_wsum[warp] = x;
     __syncthreads();
-    // decoupled look-back by warp 0: the 32 nearest predecessors' states are read at
-    // once (each wait bounded), the nearest inclusive one is found by ballot and the
-    // states up to it are summed across the warp; only a window of aggregates moves
-    // the look-back 32 tiles further
     if (warp == 0)
     {
         long long agg = 0;
         for (int w = 0; w < kScanThreads / 32; ++w)
             agg += s_wsum[w];
-        unsigned long long *st = status + tile;
-        long long excl = 0;
-        if (lane == 0)
-            st_release64(st, (tile == 0 ? kSFlagInc : kSFlagAgg) | (unsigned long long)agg);
-        if (tile > 0)
-        {
-            for (int top = tile - 1;; top -= 32)
-            {
-                const int p = top - lane;
-                unsigned long long s = kSFlagInc; // before tile 0: an inclusive zero
-                if (p >= 0)
-                {
-                    const uint32_t limit = wait_limit(d_err);
-                    uint32_t spins = 0;
-                    s = ld_acquire64(status + p);
-                    while ((s & kSFlagMask) == 0)
-                    {
-                        if (++spins > limit)
-                        {
-                            atomicOr(d_err, kErrTimeout);
-                            break;
-                        }
-                        if (spins > 64)
-                            __nanosleep(64);
-                        s = ld_acquire64(status + p);
-                    }
-                }
-                const unsigned inc = __ballot_sync(0xffffffffu, (s & kSFlagMask) != kSFlagAgg);
-                const int stop = inc ? __ffs(inc) - 1 : 31;
-                long long v = lane <= stop ? (long long)(s & kSValMask) : 0;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
-                    v += __shfl_xor_sync(0xffffffffu, v, o);
-                excl += v;
-                if (inc)
-                    break;
-            }
-            if (lane == 0)
-                st_release64(st, kSFlagInc | (unsigned long long)(excl + agg));
-        }
+        const long long excl = scan_lookback(tile, agg, status, d_err);
         if (lane == 0)
         {
             s_prefix = excl;
@@ -701,6 +675,106 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const Op op_in, const int
         if (base + i < n)
             op.put(base + i, run, (int)v[i]);
         run += v[i];
+    }
+}
+
+// the runs of equal keys of a sorted view in one pass: a tile's keys are read
+// coalesced (thread t reads elements t, t + 256, ...), each element's run start (bit 0)
+// and segment start (bit 1) go to shared memory as one byte, and every thread scans its
+// own eight consecutive bytes; a run's exclusive prefix is its index, so starts[run] is
+// its first position (starts[runs] = n) and seg_first[seg] the segment's first run
+__global__ void __launch_bounds__(kScanThreads) k_run_scan(SortBuffers sb, const KeyLayout *lay, const int32_t *d_n,
+                                                           ScanCtl *ctl, unsigned long long *status, int32_t *starts,
+                                                           int32_t *seg_first, int32_t *d_runs, int *d_err)
+{
+    __shared__ uint32_t s_tile;
+    __shared__ long long s_wsum[kScanThreads / 32];
+    __shared__ long long s_prefix;
+    __shared__ __align__(8) uint8_t s_f[kScanTile];
+    const int n = *d_n;
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    if (threadIdx.x == 0)
+        s_tile = atomicAdd(&ctl->tile_ctr, 1u);
+    __syncthreads();
+    const int tile = (int)s_tile;
+    if (tile >= ntiles)
+    {
+        if (tile == 0 && threadIdx.x == 0)
+        {
+            *d_runs = 0; // empty input
+            starts[0] = 0;
+        }
+        return;
+    }
+    const SortedView sv = sorted_view(sb);
+    const KeyLayout L = *lay;
+    const int segshift = L.bx + L.by + L.bz;
+    const int tbase = tile * kScanTile;
+#pragma unroll
+    for (int it = 0; it < kScanItems; ++it)
+    {
+        const int i = tbase + it * kScanThreads + (int)threadIdx.x;
+        uint32_t f = 0;
+        if (i < n)
+        {
+            if (i == 0)
+                f = 3;
+            else
+            {
+                const uint64_t k = sv.key(i), kp = sv.key(i - 1);
+                f = (k != kp ? 1u : 0u) | (L.bseg && (k >> segshift) != (kp >> segshift) ? 2u : 0u);
+            }
+        }
+        s_f[it * kScanThreads + threadIdx.x] = (uint8_t)f;
+    }
+    __syncthreads();
+    const int base = tbase + (int)threadIdx.x * kScanItems;
+    const uint64_t f8 = *reinterpret_cast<const uint64_t *>(&s_f[threadIdx.x * kScanItems]);
+    const long long tsum = __popcll(f8 & 0x0101010101010101ull);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    long long x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0)
+    {
+        long long agg = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w)
+            agg += s_wsum[w];
+        const long long excl = scan_lookback(tile, agg, status, d_err);
+        if (lane == 0)
+        {
+            s_prefix = excl;
+            if (tile == ntiles - 1)
+            {
+                *d_runs = (int32_t)(excl + agg);
+                starts[excl + agg] = n;
+            }
+        }
+    }
+    __syncthreads();
+    long long run = s_prefix;
+    for (int w = 0; w < warp; ++w)
+        run += s_wsum[w];
+    run += x - tsum;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j)
+    {
+        const uint32_t f = (uint32_t)(f8 >> (8 * j)) & 3u;
+        if (f & 1u)
+        {
+            starts[run] = base + j;
+            if (f & 2u || base + j == 0)
+                seg_first[L.bseg ? (int)(sv.key(base + j) >> segshift) : 0] = (int32_t)run;
+            ++run;
+        }
     }
 }
 
@@ -730,8 +804,8 @@ int run_scan(gca3d_context *ctx, const SortBuffers &sb, const int32_t *d_n, int6
         return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "run_scan: scratch");
     GCA_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(ScanCtl), ctx->stream));
     GCA_CUDA(ctx, cudaMemsetAsync(status, 0, sizeof(unsigned long long) * (ntiles > 0 ? ntiles : 1), ctx->stream));
-    k_scan<<<(int)(ntiles > 0 ? ntiles : 1), kScanThreads, 0, ctx->stream>>>(
-        RunScan{sb, lay, starts, seg_first, d_runs, SortedView{}}, d_n, ctl, status, ctx->d_err);
+    k_run_scan<<<(int)(ntiles > 0 ? ntiles : 1), kScanThreads, 0, ctx->stream>>>(sb, lay, d_n, ctl, status, starts,
+                                                                                 seg_first, d_runs, ctx->d_err);
     GCA_CHECK_LAUNCH(ctx);
     return GCA3D_OK;
 }
