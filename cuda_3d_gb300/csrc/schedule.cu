@@ -49,6 +49,11 @@ struct gca3d_icp_plan
     int64_t kernels_static = 0; // graph kernels outside the iteration loops
     bool host_checks = false; // plain mode: convergence test read back after every iteration
     cudaStream_t side = nullptr; // captures the bodies of the device-side loops
+    // the preparation branch (every scale's clouds, grids and normals) and its events:
+    // the fork after the prologue, and one per scale for the iterations to wait on
+    cudaStream_t prep = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_scale[GCA3D_MAX_SCALES] = {};
     PlanPrologue prologue;       // work enqueued before the schedule (captured with it)
     bool vox_given = false;      // voxel batches supplied by the caller
     PlanVoxels vox;
@@ -114,7 +119,106 @@ SubLevels finer_scales(const gca3d_icp_params &p, int si)
     return sub;
 }
 
-// enqueue the whole schedule on the context stream (eager or under capture)
+// what the iterations of one scale work on, made by the preparation branch
+struct ScalePrep
+{
+    Batch bs, bt;
+    Grid gicp; // the grid the correspondence search walks
+    float4 *attr0 = nullptr, *attr1 = nullptr;
+    double *partials = nullptr;
+    int2 *corr = nullptr;
+    NNCerts cert{nullptr, nullptr};
+    int *bmap = nullptr, *bmap_nn = nullptr;
+};
+
+// one scale's clouds, grids, normals, gradients and iteration scratch, enqueued on the
+// context stream; none of it depends on the pose, so it can run ahead of the iterations
+static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, VoxelChain &chain_tgt, ScalePrep &out)
+{
+    gca3d_context *ctx = pl->ctx;
+    const gca3d_icp_params &p = pl->prm;
+    const int P = pl->P;
+    int st = GCA3D_OK;
+    const gca3d_scale &S = p.scales[si];
+    const bool keep = S.voxel <= 0.0f && p.keep_target_normals;
+    Batch &bs = out.bs, &bt = out.bt;
+    if (S.voxel > 0.0f)
+    {
+        // both clouds in Z-order of their voxels: compact source work items, and the
+        // same target whether it is downsampled here or supplied
+        if (pl->vox_given)
+        {
+            bs = pl->vox.src[si];
+            bt = pl->vox.tgt[si];
+        }
+        const SubLevels sub = p.tuning.voxel_resort ? SubLevels{} : finer_scales(p, si);
+        const bool refine = chain_src.used < chain_src.levels;
+        st = refine ? voxel_refine(ctx, pl->d_src, chain_src, bs)
+                    : voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true, &sub, &chain_src);
+        if (st)
+            return st;
+        if (!pl->vox_given)
+        {
+            st = chain_tgt.used < chain_tgt.levels
+                     ? voxel_refine(ctx, pl->d_tgt, chain_tgt, bt)
+                     : voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt, true, &sub, &chain_tgt);
+            if (st)
+                return st;
+        }
+    }
+    else
+    {
+        if ((st = batch_alloc(ctx, bs, P, pl->src_cap, pl->src_max, false, false)))
+            return st;
+        if ((st = gather_stage(ctx, pl->d_src, P, pl->src_max, bs, false)))
+            return st;
+        if ((st = batch_alloc(ctx, bt, P, pl->tgt_cap, pl->tgt_max, keep, false)))
+            return st;
+        if ((st = gather_stage(ctx, pl->d_tgt, P, pl->tgt_max, bt, keep)))
+            return st;
+    }
+    // the normals / gradient grid (cell = largest of their radii) and, when the
+    // correspondence distance is smaller, a tighter grid for the NN search
+    float cell_n = S.grad_radius;
+    if (!keep)
+        cell_n = std::max(cell_n, S.normal_radius);
+    const bool own_nn_grid = S.max_corr < 0.9f * cell_n;
+    Grid g, gnn;
+    if ((st = grid_build(ctx, bt, std::max(cell_n, own_nn_grid ? 0.0f : S.max_corr), kOriginPadF32, nullptr, g)))
+        return st;
+    if (own_nn_grid && (st = grid_build(ctx, bt, S.max_corr, kOriginPadF32, nullptr, gnn)))
+        return st;
+    out.gicp = own_nn_grid ? gnn : g;
+    float4 *attr0 = out.attr0 = ctx->arena.get<float4>(g.cap);
+    float4 *attr1 = out.attr1 = ctx->arena.get<float4>(g.cap);
+    double *partials = out.partials = ctx->arena.get<double>((size_t)std::max(pl->max_blocks, 1) * kTermsPad);
+    int2 *corr = out.corr = ctx->arena.get<int2>(std::max<int64_t>(bs.cap, 1));
+    const NNCerts cert = out.cert = NNCerts{ctx->arena.get<float4>(std::max<int64_t>(bs.cap, 1)),
+                                            ctx->arena.get<int>(std::max<int64_t>(bs.cap, 1))};
+    int *bmap = out.bmap = ctx->arena.get<int>(P + 2); // offsets, total, active pairs
+    int *bmap_nn = out.bmap_nn = ctx->arena.get<int>(P + 2); // offsets, total, work queue
+    float4 *nrm_b = own_nn_grid && !keep ? ctx->arena.get<float4>(g.cap) : nullptr;
+    float4 *grd_b = own_nn_grid ? ctx->arena.get<float4>(g.cap) : nullptr;
+    if (!attr0 || !attr1 || !partials || !corr || !cert.pos || !cert.t || !bmap || !bmap_nn || (own_nn_grid && (!grd_b || (!keep && !nrm_b))))
+        return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
+    if (own_nn_grid)
+    {
+        if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
+                                keep ? bt.nrm : nullptr, nullptr, nullptr, nrm_b, grd_b)))
+            return st;
+        if ((st = gather_attrs(ctx, bt, gnn, keep ? bt.nrm : nrm_b, grd_b, attr0, attr1)))
+            return st;
+    }
+    else if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
+                                 keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
+        return st;
+    return GCA3D_OK;
+}
+
+// enqueue the whole schedule (eager or under capture): the preparation of every scale
+// on the plan's preparation stream, forked from the context stream after the prologue,
+// and the iterations on the context stream, each scale's after its preparation; the
+// last scale's event joins the two streams again
 int run_schedule(gca3d_icp_plan *pl, bool capturing)
 {
     gca3d_context *ctx = pl->ctx;
@@ -123,160 +227,128 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
     int st = icp_state_init(ctx, pl->d_state, P, pl->d_Tinit);
     if (st)
         return st;
-    VoxelChain chain_src, chain_tgt; // sorted state of the last voxel stage, for finer scales
-    for (int si = 0; si < p.n_scales; ++si)
+    cudaStream_t main_stream = ctx->stream;
+    GCA_CUDA(ctx, cudaEventRecord(pl->ev_fork, main_stream));
+    GCA_CUDA(ctx, cudaStreamWaitEvent(pl->prep, pl->ev_fork, 0));
+    ScalePrep sp[GCA3D_MAX_SCALES];
     {
-        const gca3d_scale &S = p.scales[si];
-        const bool keep = S.voxel <= 0.0f && p.keep_target_normals;
-        Batch bs, bt;
-        if (S.voxel > 0.0f)
+        VoxelChain chain_src, chain_tgt; // sorted state of the last voxel stage, for finer scales
+        ctx->stream = pl->prep;
+        for (int si = 0; si < p.n_scales && !st; ++si)
         {
-            // both clouds in Z-order of their voxels: compact source work items, and the
-            // same target whether it is downsampled here or supplied
-            if (pl->vox_given)
+            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si]);
+            if (!st)
             {
-                bs = pl->vox.src[si];
-                bt = pl->vox.tgt[si];
-            }
-            const SubLevels sub = p.tuning.voxel_resort ? SubLevels{} : finer_scales(p, si);
-            const bool refine = chain_src.used < chain_src.levels;
-            st = refine ? voxel_refine(ctx, pl->d_src, chain_src, bs)
-                        : voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true, &sub, &chain_src);
-            if (st)
-                return st;
-            if (!pl->vox_given)
-            {
-                st = chain_tgt.used < chain_tgt.levels
-                         ? voxel_refine(ctx, pl->d_tgt, chain_tgt, bt)
-                         : voxel_stage(ctx, pl->d_tgt, P, pl->tgt_cap, pl->tgt_max, S.voxel, bt, true, &sub, &chain_tgt);
-                if (st)
-                    return st;
+                const cudaError_t e = cudaEventRecord(pl->ev_scale[si], pl->prep);
+                if (e != cudaSuccess)
+                    st = cuda_fail(ctx, e, "icp: preparation event");
             }
         }
-        else
+        ctx->stream = main_stream;
+        if (st)
         {
-            if ((st = batch_alloc(ctx, bs, P, pl->src_cap, pl->src_max, false, false)))
-                return st;
-            if ((st = gather_stage(ctx, pl->d_src, P, pl->src_max, bs, false)))
-                return st;
-            if ((st = batch_alloc(ctx, bt, P, pl->tgt_cap, pl->tgt_max, keep, false)))
-                return st;
-            if ((st = gather_stage(ctx, pl->d_tgt, P, pl->tgt_max, bt, keep)))
-                return st;
-        }
-        // the normals / gradient grid (cell = largest of their radii) and, when the
-        // correspondence distance is smaller, a tighter grid for the NN search
-        float cell_n = S.grad_radius;
-        if (!keep)
-            cell_n = std::max(cell_n, S.normal_radius);
-        const bool own_nn_grid = S.max_corr < 0.9f * cell_n;
-        Grid g, gnn;
-        if ((st = grid_build(ctx, bt, std::max(cell_n, own_nn_grid ? 0.0f : S.max_corr), kOriginPadF32, nullptr, g)))
+            // join the branch before giving up (a capture must end on one stream)
+            cudaEventRecord(pl->ev_fork, pl->prep);
+            cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
             return st;
-        if (own_nn_grid && (st = grid_build(ctx, bt, S.max_corr, kOriginPadF32, nullptr, gnn)))
-            return st;
-        const Grid &gicp = own_nn_grid ? gnn : g;
-        float4 *attr0 = ctx->arena.get<float4>(g.cap);
-        float4 *attr1 = ctx->arena.get<float4>(g.cap);
-        double *partials = ctx->arena.get<double>((size_t)std::max(pl->max_blocks, 1) * kTermsPad);
-        int2 *corr = ctx->arena.get<int2>(std::max<int64_t>(bs.cap, 1));
-        const NNCerts cert{ctx->arena.get<float4>(std::max<int64_t>(bs.cap, 1)),
-                           ctx->arena.get<int>(std::max<int64_t>(bs.cap, 1))};
-        int *bmap = ctx->arena.get<int>(P + 2); // offsets, total, active pairs
-        int *bmap_nn = ctx->arena.get<int>(P + 2); // offsets, total, work queue
-        float4 *nrm_b = own_nn_grid && !keep ? ctx->arena.get<float4>(g.cap) : nullptr;
-        float4 *grd_b = own_nn_grid ? ctx->arena.get<float4>(g.cap) : nullptr;
-        if (!attr0 || !attr1 || !partials || !corr || !cert.pos || !cert.t || !bmap || !bmap_nn || (own_nn_grid && (!grd_b || (!keep && !nrm_b))))
-            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
-        if (own_nn_grid)
-        {
-            if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
-                                    keep ? bt.nrm : nullptr, nullptr, nullptr, nrm_b, grd_b)))
-                return st;
-            if ((st = gather_attrs(ctx, bt, gnn, keep ? bt.nrm : nrm_b, grd_b, attr0, attr1)))
-                return st;
-        }
-        else if ((st = normals_stage(ctx, bt, g, !keep, S.normal_radius, S.max_nn, true, S.grad_radius,
-                                     keep ? bt.nrm : nullptr, attr0, attr1, nullptr, nullptr)))
-            return st;
-        const IcpShape shape = icp_shape(p.tuning);
-        if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, bmap_nn, si, shape.nn_chunk)))
-            return st;
-        IcpScale prm;
-        prm.max_corr = S.max_corr;
-        prm.sqrt_lg = sqrtf(p.lambda);
-        prm.sqrt_lc = sqrtf(1.0f - p.lambda);
-        prm.update_map = p.update_map;
-        prm.rot_eps = p.rot_eps;
-        prm.trans_eps = p.trans_eps;
-        // loop counter and finalize ticket
-        int *iter = ctx->arena.get<int>(2);
-        if (!iter)
-            return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
-        GCA_CUDA(ctx, cudaMemsetAsync(iter, 0, 2 * sizeof(int), ctx->stream));
-        IcpLoop loop;
-        loop.ticket = reinterpret_cast<unsigned *>(iter + 1);
-        if (capturing && S.max_iter > 0)
-        {
-            // the iteration loop as a device-side WHILE node: the body runs while a
-            // pair is active and the budget lasts, so converged schedules stop early
-            cudaStreamCaptureStatus cs;
-            cudaGraph_t cg = nullptr;
-            const cudaGraphNode_t *deps = nullptr;
-            size_t nd = 0;
-            GCA_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, nullptr, &nd));
-            cudaGraphConditionalHandle handle;
-            GCA_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault));
-            cudaGraphNodeParams np = {};
-            np.type = cudaGraphNodeTypeConditional;
-            np.conditional.handle = handle;
-            np.conditional.type = cudaGraphCondTypeWhile;
-            np.conditional.size = 1;
-            cudaGraphNode_t node;
-            GCA_CUDA(ctx, cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np));
-            cudaGraph_t body = np.conditional.phGraph_out[0];
-            cudaStream_t main_stream = ctx->stream;
-            GCA_CUDA(ctx, cudaStreamBeginCaptureToGraph(pl->side, body, nullptr, nullptr, 0,
-                                                        cudaStreamCaptureModeThreadLocal));
-            ctx->stream = pl->side;
-            const int64_t l0 = ctx->launches;
-            loop.handle = handle;
-            loop.iter = iter;
-            loop.max_iter = S.max_iter;
-            st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                               pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr, loop,
-                               shape);
-            pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
-            ctx->stream = main_stream;
-            cudaGraph_t captured = nullptr;
-            const cudaError_t e = cudaStreamEndCapture(pl->side, &captured);
-            if (st)
-                return st;
-            GCA_CUDA(ctx, e);
-            GCA_CUDA(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1,
-                                                              cudaStreamSetCaptureDependencies));
-            continue;
-        }
-        for (int it = 0; it < S.max_iter; ++it)
-        {
-            if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                                    pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr,
-                                    loop, shape)))
-                return st;
-            if (pl->host_checks && !capturing)
-            {
-                // the reference's control flow: the step is inspected on the host
-                if ((st = read_states(pl)))
-                    return st;
-                bool any = false;
-                for (int k = 0; k < P; ++k)
-                    any |= pl->h_state[k].active != 0;
-                if (!any)
-                    break;
-            }
         }
     }
-    return GCA3D_OK;
+    // the iterations, each scale's after its preparation
+    auto iterate = [&]() -> int {
+        for (int si = 0; si < p.n_scales; ++si)
+        {
+            const gca3d_scale &S = p.scales[si];
+            GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
+            const Batch &bs = sp[si].bs, &bt = sp[si].bt;
+            const Grid &gicp = sp[si].gicp;
+            float4 *attr0 = sp[si].attr0, *attr1 = sp[si].attr1;
+            double *partials = sp[si].partials;
+            int2 *corr = sp[si].corr;
+            const NNCerts cert = sp[si].cert;
+            int *bmap = sp[si].bmap, *bmap_nn = sp[si].bmap_nn;
+            const IcpShape shape = icp_shape(p.tuning);
+            if ((st = icp_setup(ctx, pl->d_state, P, bs.seg_off, bt.seg_off, bmap, bmap_nn, si, shape.nn_chunk)))
+                return st;
+            IcpScale prm;
+            prm.max_corr = S.max_corr;
+            prm.sqrt_lg = sqrtf(p.lambda);
+            prm.sqrt_lc = sqrtf(1.0f - p.lambda);
+            prm.update_map = p.update_map;
+            prm.rot_eps = p.rot_eps;
+            prm.trans_eps = p.trans_eps;
+            // loop counter and finalize ticket
+            int *iter = ctx->arena.get<int>(2);
+            if (!iter)
+                return fail(ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp: scratch");
+            GCA_CUDA(ctx, cudaMemsetAsync(iter, 0, 2 * sizeof(int), ctx->stream));
+            IcpLoop loop;
+            loop.ticket = reinterpret_cast<unsigned *>(iter + 1);
+            if (capturing && S.max_iter > 0)
+            {
+                // the iteration loop as a device-side WHILE node: the body runs while a
+                // pair is active and the budget lasts, so converged schedules stop early
+                cudaStreamCaptureStatus cs;
+                cudaGraph_t cg = nullptr;
+                const cudaGraphNode_t *deps = nullptr;
+                size_t nd = 0;
+                GCA_CUDA(ctx, cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, &cg, &deps, nullptr, &nd));
+                cudaGraphConditionalHandle handle;
+                GCA_CUDA(ctx, cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault));
+                cudaGraphNodeParams np = {};
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = handle;
+                np.conditional.type = cudaGraphCondTypeWhile;
+                np.conditional.size = 1;
+                cudaGraphNode_t node;
+                GCA_CUDA(ctx, cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np));
+                cudaGraph_t body = np.conditional.phGraph_out[0];
+                GCA_CUDA(ctx, cudaStreamBeginCaptureToGraph(pl->side, body, nullptr, nullptr, 0,
+                                                            cudaStreamCaptureModeThreadLocal));
+                ctx->stream = pl->side;
+                const int64_t l0 = ctx->launches;
+                loop.handle = handle;
+                loop.iter = iter;
+                loop.max_iter = S.max_iter;
+                st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
+                                   pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr, loop,
+                                   shape);
+                pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
+                ctx->stream = main_stream;
+                cudaGraph_t captured = nullptr;
+                const cudaError_t e = cudaStreamEndCapture(pl->side, &captured);
+                if (st)
+                    return st;
+                GCA_CUDA(ctx, e);
+                GCA_CUDA(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1,
+                                                                  cudaStreamSetCaptureDependencies));
+                continue;
+            }
+            for (int it = 0; it < S.max_iter; ++it)
+            {
+                if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
+                                        pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr,
+                                        loop, shape)))
+                    return st;
+                if (pl->host_checks && !capturing)
+                {
+                    // the reference's control flow: the step is inspected on the host
+                    if ((st = read_states(pl)))
+                        return st;
+                    bool any = false;
+                    for (int k = 0; k < P; ++k)
+                        any |= pl->h_state[k].active != 0;
+                    if (!any)
+                        break;
+                }
+            }
+        }
+
+        return GCA3D_OK;
+    };
+    st = iterate();
+    if (st) // join the branch before giving up
+        cudaStreamWaitEvent(main_stream, pl->ev_scale[p.n_scales - 1], 0);
+    return st;
 }
 
 int run_with_arena(gca3d_icp_plan *pl, bool capturing)
@@ -341,6 +413,13 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
         cudaFreeHost(pl->h_err);
     if (pl->side)
         cudaStreamDestroy(pl->side);
+    if (pl->prep)
+        cudaStreamDestroy(pl->prep);
+    if (pl->ev_fork)
+        cudaEventDestroy(pl->ev_fork);
+    for (cudaEvent_t e : pl->ev_scale)
+        if (e)
+            cudaEventDestroy(e);
     if (pl->graph)
         cudaGraphDestroy(pl->graph);
     cudaFree(pl->d_src);
@@ -441,6 +520,16 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
         cudaGetLastError();
         gca3d_icp_plan_destroy(pl);
         return fail(ctx, GCA3D_ERR_CUDA, "icp plan: side stream");
+    }
+    bool events_ok = cudaStreamCreateWithFlags(&pl->prep, cudaStreamNonBlocking) == cudaSuccess &&
+                     cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < params->n_scales && events_ok; ++k)
+        events_ok = cudaEventCreateWithFlags(&pl->ev_scale[k], cudaEventDisableTiming) == cudaSuccess;
+    if (!events_ok)
+    {
+        cudaGetLastError();
+        gca3d_icp_plan_destroy(pl);
+        return fail(ctx, GCA3D_ERR_CUDA, "icp plan: preparation stream");
     }
     if (capture)
     {
