@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 #include <utility>
+#include <vector>
 
 using namespace gca3d;
 
@@ -54,6 +55,7 @@ struct gca3d_icp_plan
     cudaStream_t prep = nullptr;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_scale[GCA3D_MAX_SCALES] = {};
+    int priority = 0; // the device's greatest stream priority (the iterations' kernels)
     PlanPrologue prologue;       // work enqueued before the schedule (captured with it)
     bool vox_given = false;      // voxel batches supplied by the caller
     PlanVoxels vox;
@@ -215,6 +217,31 @@ static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, Voxe
     return GCA3D_OK;
 }
 
+// give every kernel node of a graph the launch priority prio
+static cudaError_t prioritise_kernels(cudaGraph_t graph, int prio)
+{
+    size_t n = 0;
+    cudaError_t e = cudaGraphGetNodes(graph, nullptr, &n);
+    if (e != cudaSuccess || n == 0)
+        return e;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if ((e = cudaGraphGetNodes(graph, nodes.data(), &n)) != cudaSuccess)
+        return e;
+    for (cudaGraphNode_t node : nodes)
+    {
+        cudaGraphNodeType type;
+        if ((e = cudaGraphNodeGetType(node, &type)) != cudaSuccess)
+            return e;
+        if (type != cudaGraphNodeTypeKernel)
+            continue;
+        cudaKernelNodeAttrValue v = {};
+        v.priority = prio;
+        if ((e = cudaGraphKernelNodeSetAttribute(node, cudaLaunchAttributePriority, &v)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
 // enqueue the whole schedule (eager or under capture): the preparation of every scale
 // on the plan's preparation stream, forked from the context stream after the prologue,
 // and the iterations on the context stream, each scale's after its preparation; the
@@ -319,6 +346,9 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
                 if (st)
                     return st;
                 GCA_CUDA(ctx, e);
+                // the iterations are the critical path: their kernels go first where the
+                // preparation branch's kernels compete for the same SMs
+                GCA_CUDA(ctx, prioritise_kernels(body, pl->priority));
                 GCA_CUDA(ctx, cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1,
                                                                   cudaStreamSetCaptureDependencies));
                 continue;
@@ -521,6 +551,9 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
         gca3d_icp_plan_destroy(pl);
         return fail(ctx, GCA3D_ERR_CUDA, "icp plan: side stream");
     }
+    int least_prio = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least_prio, &pl->priority) != cudaSuccess)
+        pl->priority = 0;
     bool events_ok = cudaStreamCreateWithFlags(&pl->prep, cudaStreamNonBlocking) == cudaSuccess &&
                      cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
     for (int k = 0; k < params->n_scales && events_ok; ++k)
@@ -558,7 +591,7 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
                     st = cuda_fail(ctx, e, "cudaStreamEndCapture");
                 else
                 {
-                    e = cudaGraphInstantiate(&pl->exec, pl->graph, 0);
+                    e = cudaGraphInstantiate(&pl->exec, pl->graph, cudaGraphInstantiateFlagUseNodePriority);
                     if (e != cudaSuccess)
                         st = cuda_fail(ctx, e, "cudaGraphInstantiate");
                     // until an execute reports iteration counts: every loop runs to its budget
