@@ -255,18 +255,24 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
     if (st)
         return st;
     cudaStream_t main_stream = ctx->stream;
-    GCA_CUDA(ctx, cudaEventRecord(pl->ev_fork, main_stream));
-    GCA_CUDA(ctx, cudaStreamWaitEvent(pl->prep, pl->ev_fork, 0));
+    // serial: the preparation on the context stream itself (no branch, nothing overlaps)
+    const bool serial = p.tuning.serial_prep != 0;
+    cudaStream_t prep = serial ? main_stream : pl->prep;
+    if (!serial)
+    {
+        GCA_CUDA(ctx, cudaEventRecord(pl->ev_fork, main_stream));
+        GCA_CUDA(ctx, cudaStreamWaitEvent(prep, pl->ev_fork, 0));
+    }
     ScalePrep sp[GCA3D_MAX_SCALES];
     {
         VoxelChain chain_src, chain_tgt; // sorted state of the last voxel stage, for finer scales
-        ctx->stream = pl->prep;
+        ctx->stream = prep;
         for (int si = 0; si < p.n_scales && !st; ++si)
         {
             st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si]);
-            if (!st)
+            if (!st && !serial)
             {
-                const cudaError_t e = cudaEventRecord(pl->ev_scale[si], pl->prep);
+                const cudaError_t e = cudaEventRecord(pl->ev_scale[si], prep);
                 if (e != cudaSuccess)
                     st = cuda_fail(ctx, e, "icp: preparation event");
             }
@@ -274,9 +280,12 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         ctx->stream = main_stream;
         if (st)
         {
-            // join the branch before giving up (a capture must end on one stream)
-            cudaEventRecord(pl->ev_fork, pl->prep);
-            cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
+            if (!serial)
+            {
+                // join the branch before giving up (a capture must end on one stream)
+                cudaEventRecord(pl->ev_fork, prep);
+                cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
+            }
             return st;
         }
     }
@@ -285,7 +294,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         for (int si = 0; si < p.n_scales; ++si)
         {
             const gca3d_scale &S = p.scales[si];
-            GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
+            if (!serial)
+                GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
             const Batch &bs = sp[si].bs, &bt = sp[si].bt;
             const Grid &gicp = sp[si].gicp;
             float4 *attr0 = sp[si].attr0, *attr1 = sp[si].attr1;
@@ -376,7 +386,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         return GCA3D_OK;
     };
     st = iterate();
-    if (st) // join the branch before giving up
+    if (st && !serial) // join the branch before giving up
         cudaStreamWaitEvent(main_stream, pl->ev_scale[p.n_scales - 1], 0);
     return st;
 }
@@ -740,7 +750,8 @@ extern "C" int gca3d_icp_autotune(gca3d_context *ctx, int n_pairs, gca3d_cloud *
     reps = std::max(reps, 1);
     gca3d_icp_params p = *params;
     const IcpShape s0 = icp_shape(p.tuning);
-    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps, p.tuning.voxel_resort, s0.fused ? 1 : 0};
+    gca3d_tuning cur{s0.nn_chunk, s0.nn_bps, s0.acc_bps, p.tuning.voxel_resort, s0.fused ? 1 : 0,
+                     p.tuning.serial_prep};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     {

@@ -50,7 +50,8 @@ class ScaleParams(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("nn_item_points", C.c_int), ("nn_blocks_per_sm", C.c_int), ("accum_blocks_per_sm", C.c_int),
-                ("voxel_resort", C.c_int), ("fused_finalize", C.c_int)]
+                ("voxel_resort", C.c_int), ("fused_finalize", C.c_int),
+                ("serial_prep", C.c_int)]
 
 
 class IcpParams(C.Structure):

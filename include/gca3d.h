@@ -91,6 +91,9 @@ typedef struct {
                                 carries their sub-cell bits and each finer scale splits its runs */
     int fused_finalize;      /* 1: the last accumulate block of each pair runs the pair's solve and
                                 pose update; 0 (default): they are a launch of their own */
+    int serial_prep;         /* 1: every scale's clouds, grids and normals on the context stream,
+                                before its iterations; 0 (default): on a branch of their own that
+                                runs ahead, so finer scales are prepared while coarser ones iterate */
 } gca3d_tuning;
 
 typedef struct {

@@ -241,6 +241,27 @@ def test_autotune_and_every_launch_shape_give_identical_results(ctx, N, synth):
             assert a["iterations"] == b["iterations"]
 
 
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_preparation_branch_changes_no_bit(ctx, N, synth, use_graph):
+    """Every scale's clouds, grids and normals prepared on a branch of their own that runs
+    ahead of the iterations (default) or on the context stream before each scale's
+    iterations: the same kernels on the same data, so the same bits."""
+    pairs = synth.batch_pairs(10, seed=7, n_min=10_000, n_max=80_000)
+    srcs = [ctx.cloud_from(p.src_xyz, p.src_rgb) for p in pairs]
+    tgts = [ctx.cloud_from(p.tgt_xyz, p.tgt_rgb) for p in pairs]
+    out = []
+    for serial in (0, 1):
+        prm = N.icp_params(c1_scales(N), update_map=N.UPDATE_SE3_EXP, use_graph=use_graph,
+                           tuning=N.Tuning(0, 0, 0, 0, 0, serial))
+        plan = N.IcpPlan(ctx, srcs, tgts, prm)
+        out.append([plan.execute(results=True) for _ in range(2)])
+    for run0, run1 in zip(*out):
+        for a, b in zip(run0, run1):
+            np.testing.assert_array_equal(a["T"], b["T"])
+            for k in ("iterations", "fitness", "inlier_rmse", "rmse_ref", "scale_iterations", "scale_n_src"):
+                assert a[k] == b[k], k
+
+
 def test_queued_executes_read_their_own_results(ctx, N, synth):
     """Two plans executed back to back without waiting: each plan's results() waits
     for its own execute (the state copy queued behind it) and returns that execute's
