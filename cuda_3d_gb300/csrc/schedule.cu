@@ -55,6 +55,12 @@ struct gca3d_icp_plan
     cudaStream_t prep = nullptr;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_scale[GCA3D_MAX_SCALES] = {};
+    // with a supplied target and a prologue (the tracker: the prologue makes the new
+    // frame, the target is the previous one), the source preparation has a branch of
+    // its own, forked after the prologue, while the target's starts before it
+    cudaStream_t prep_src = nullptr;
+    cudaEvent_t ev_fork_src = nullptr;
+    cudaEvent_t ev_src[GCA3D_MAX_SCALES] = {};
     int priority = 0; // the device's greatest stream priority (the iterations' kernels)
     PlanPrologue prologue;       // work enqueued before the schedule (captured with it)
     bool vox_given = false;      // voxel batches supplied by the caller
@@ -134,8 +140,10 @@ struct ScalePrep
 };
 
 // one scale's clouds, grids, normals, gradients and iteration scratch, enqueued on the
-// context stream; none of it depends on the pose, so it can run ahead of the iterations
-static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, VoxelChain &chain_tgt, ScalePrep &out)
+// context stream (the source's on src_stream); none of it depends on the pose, so it can
+// run ahead of the iterations
+static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, VoxelChain &chain_tgt, ScalePrep &out,
+                         cudaStream_t src_stream)
 {
     gca3d_context *ctx = pl->ctx;
     const gca3d_icp_params &p = pl->prm;
@@ -155,8 +163,11 @@ static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, Voxe
         }
         const SubLevels sub = p.tuning.voxel_resort ? SubLevels{} : finer_scales(p, si);
         const bool refine = chain_src.used < chain_src.levels;
+        cudaStream_t tgt_stream = ctx->stream;
+        ctx->stream = src_stream;
         st = refine ? voxel_refine(ctx, pl->d_src, chain_src, bs)
                     : voxel_stage(ctx, pl->d_src, P, pl->src_cap, pl->src_max, S.voxel, bs, true, &sub, &chain_src);
+        ctx->stream = tgt_stream;
         if (st)
             return st;
         if (!pl->vox_given)
@@ -172,7 +183,11 @@ static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, Voxe
     {
         if ((st = batch_alloc(ctx, bs, P, pl->src_cap, pl->src_max, false, false)))
             return st;
-        if ((st = gather_stage(ctx, pl->d_src, P, pl->src_max, bs, false)))
+        cudaStream_t tgt_stream = ctx->stream;
+        ctx->stream = src_stream;
+        st = gather_stage(ctx, pl->d_src, P, pl->src_max, bs, false);
+        ctx->stream = tgt_stream;
+        if (st)
             return st;
         if ((st = batch_alloc(ctx, bt, P, pl->tgt_cap, pl->tgt_max, keep, false)))
             return st;
@@ -242,26 +257,45 @@ static cudaError_t prioritise_kernels(cudaGraph_t graph, int prio)
     return cudaSuccess;
 }
 
-// enqueue the whole schedule (eager or under capture): the preparation of every scale
-// on the plan's preparation stream, forked from the context stream after the prologue,
-// and the iterations on the context stream, each scale's after its preparation; the
-// last scale's event joins the two streams again
+// enqueue the whole schedule (eager or under capture): the prologue, the preparation of
+// every scale on the plan's preparation stream, forked from the context stream after
+// the prologue (with a supplied target, the target's part forked before it and the
+// source's on a branch of its own), and the iterations on the context stream, each
+// scale's after its preparation; the last scale's events join the streams again
 int run_schedule(gca3d_icp_plan *pl, bool capturing)
 {
     gca3d_context *ctx = pl->ctx;
     const gca3d_icp_params &p = pl->prm;
     const int P = pl->P;
-    int st = icp_state_init(ctx, pl->d_state, P, pl->d_Tinit);
-    if (st)
-        return st;
     cudaStream_t main_stream = ctx->stream;
     // serial: the preparation on the context stream itself (no branch, nothing overlaps)
     const bool serial = p.tuning.serial_prep != 0;
+    const bool split = !serial && pl->prep_src != nullptr;
     cudaStream_t prep = serial ? main_stream : pl->prep;
-    if (!serial)
+    cudaStream_t prep_src = split ? pl->prep_src : prep;
+    int st = GCA3D_OK;
+    if (split)
     {
+        // the supplied target needs nothing from the prologue
         GCA_CUDA(ctx, cudaEventRecord(pl->ev_fork, main_stream));
         GCA_CUDA(ctx, cudaStreamWaitEvent(prep, pl->ev_fork, 0));
+    }
+    if (pl->prologue && (st = pl->prologue(ctx)))
+    {
+        if (split)
+        {
+            cudaEventRecord(pl->ev_fork, prep);
+            cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
+        }
+        return st;
+    }
+    if ((st = icp_state_init(ctx, pl->d_state, P, pl->d_Tinit)))
+        return st;
+    if (!serial)
+    {
+        cudaEvent_t fork = split ? pl->ev_fork_src : pl->ev_fork;
+        GCA_CUDA(ctx, cudaEventRecord(fork, main_stream));
+        GCA_CUDA(ctx, cudaStreamWaitEvent(prep_src, fork, 0));
     }
     ScalePrep sp[GCA3D_MAX_SCALES];
     {
@@ -269,10 +303,12 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         ctx->stream = prep;
         for (int si = 0; si < p.n_scales && !st; ++si)
         {
-            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si]);
+            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si], prep_src);
             if (!st && !serial)
             {
-                const cudaError_t e = cudaEventRecord(pl->ev_scale[si], prep);
+                cudaError_t e = cudaEventRecord(pl->ev_scale[si], prep);
+                if (e == cudaSuccess && split)
+                    e = cudaEventRecord(pl->ev_src[si], prep_src);
                 if (e != cudaSuccess)
                     st = cuda_fail(ctx, e, "icp: preparation event");
             }
@@ -282,9 +318,14 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         {
             if (!serial)
             {
-                // join the branch before giving up (a capture must end on one stream)
+                // join the branches before giving up (a capture must end on one stream)
                 cudaEventRecord(pl->ev_fork, prep);
                 cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
+                if (split)
+                {
+                    cudaEventRecord(pl->ev_fork_src, prep_src);
+                    cudaStreamWaitEvent(main_stream, pl->ev_fork_src, 0);
+                }
             }
             return st;
         }
@@ -296,6 +337,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             const gca3d_scale &S = p.scales[si];
             if (!serial)
                 GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
+            if (split)
+                GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_src[si], 0));
             const Batch &bs = sp[si].bs, &bt = sp[si].bt;
             const Grid &gicp = sp[si].gicp;
             float4 *attr0 = sp[si].attr0, *attr1 = sp[si].attr1;
@@ -386,8 +429,12 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         return GCA3D_OK;
     };
     st = iterate();
-    if (st && !serial) // join the branch before giving up
+    if (st && !serial) // join the branches before giving up
+    {
         cudaStreamWaitEvent(main_stream, pl->ev_scale[p.n_scales - 1], 0);
+        if (split)
+            cudaStreamWaitEvent(main_stream, pl->ev_src[p.n_scales - 1], 0);
+    }
     return st;
 }
 
@@ -397,9 +444,7 @@ int run_with_arena(gca3d_icp_plan *pl, bool capturing)
     pl->ctx->arena.reset();
     const int64_t l0 = pl->ctx->launches;
     pl->kernels_static = 0;
-    int st = pl->prologue ? pl->prologue(pl->ctx) : GCA3D_OK;
-    if (!st)
-        st = run_schedule(pl, capturing);
+    int st = run_schedule(pl, capturing);
     if (!st && pl->ctx->arena.failed)
         st = fail(pl->ctx, GCA3D_ERR_OUT_OF_MEMORY, "icp plan: scratch memory");
     pl->kernels_per_run = pl->ctx->launches - l0;
@@ -455,6 +500,13 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
         cudaStreamDestroy(pl->side);
     if (pl->prep)
         cudaStreamDestroy(pl->prep);
+    if (pl->prep_src)
+        cudaStreamDestroy(pl->prep_src);
+    if (pl->ev_fork_src)
+        cudaEventDestroy(pl->ev_fork_src);
+    for (cudaEvent_t e : pl->ev_src)
+        if (e)
+            cudaEventDestroy(e);
     if (pl->ev_fork)
         cudaEventDestroy(pl->ev_fork);
     for (cudaEvent_t e : pl->ev_scale)
@@ -568,6 +620,13 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
                      cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
     for (int k = 0; k < params->n_scales && events_ok; ++k)
         events_ok = cudaEventCreateWithFlags(&pl->ev_scale[k], cudaEventDisableTiming) == cudaSuccess;
+    if (events_ok && pl->vox_given && pl->prologue)
+    {
+        events_ok = cudaStreamCreateWithFlags(&pl->prep_src, cudaStreamNonBlocking) == cudaSuccess &&
+                    cudaEventCreateWithFlags(&pl->ev_fork_src, cudaEventDisableTiming) == cudaSuccess;
+        for (int k = 0; k < params->n_scales && events_ok; ++k)
+            events_ok = cudaEventCreateWithFlags(&pl->ev_src[k], cudaEventDisableTiming) == cudaSuccess;
+    }
     if (!events_ok)
     {
         cudaGetLastError();
