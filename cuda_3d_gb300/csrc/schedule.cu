@@ -55,9 +55,8 @@ struct gca3d_icp_plan
     cudaStream_t prep = nullptr;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_scale[GCA3D_MAX_SCALES] = {};
-    // with a supplied target and a prologue (the tracker: the prologue makes the new
-    // frame, the target is the previous one), the source preparation has a branch of
-    // its own, forked after the prologue, while the target's starts before it
+    // the source preparation's branch (the first scale's; every scale's in a tracker plan,
+    // where the prologue makes the new frame and the target is the previous one)
     cudaStream_t prep_src = nullptr;
     cudaEvent_t ev_fork_src = nullptr;
     cudaEvent_t ev_src[GCA3D_MAX_SCALES] = {};
@@ -268,34 +267,52 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
     const gca3d_icp_params &p = pl->prm;
     const int P = pl->P;
     cudaStream_t main_stream = ctx->stream;
-    // serial: the preparation on the context stream itself (no branch, nothing overlaps)
+    // serial: the preparation on the context stream itself (no branch, nothing overlaps).
+    // Otherwise the source clouds of the first scale -- and, in a tracker plan, of every
+    // scale -- are prepared on a branch of their own beside the target's: nothing else
+    // runs before the first scale's iterations, so that preparation is on the critical
+    // path.  In a tracker plan the supplied target forks before the prologue.
     const bool serial = p.tuning.serial_prep != 0;
-    const bool split = !serial && pl->prep_src != nullptr;
+    const bool tracker = !serial && pl->vox_given && pl->prologue;
     cudaStream_t prep = serial ? main_stream : pl->prep;
-    cudaStream_t prep_src = split ? pl->prep_src : prep;
+    cudaStream_t prep_src = serial ? main_stream : pl->prep_src;
+    auto src_branch = [&](int si) { return !serial && (tracker || si == 0); };
     int st = GCA3D_OK;
-    if (split)
+    auto join = [&](int last) {
+        // join the branches before giving up (a capture must end on one stream)
+        if (serial)
+            return;
+        cudaEventRecord(pl->ev_fork, prep);
+        cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
+        if (last >= 0)
+        {
+            cudaEventRecord(pl->ev_fork_src, prep_src);
+            cudaStreamWaitEvent(main_stream, pl->ev_fork_src, 0);
+        }
+    };
+    if (tracker)
     {
-        // the supplied target needs nothing from the prologue
         GCA_CUDA(ctx, cudaEventRecord(pl->ev_fork, main_stream));
         GCA_CUDA(ctx, cudaStreamWaitEvent(prep, pl->ev_fork, 0));
     }
     if (pl->prologue && (st = pl->prologue(ctx)))
     {
-        if (split)
-        {
-            cudaEventRecord(pl->ev_fork, prep);
-            cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
-        }
+        if (tracker)
+            join(-1);
         return st;
     }
     if ((st = icp_state_init(ctx, pl->d_state, P, pl->d_Tinit)))
+    {
+        if (tracker)
+            join(-1);
         return st;
+    }
     if (!serial)
     {
-        cudaEvent_t fork = split ? pl->ev_fork_src : pl->ev_fork;
-        GCA_CUDA(ctx, cudaEventRecord(fork, main_stream));
-        GCA_CUDA(ctx, cudaStreamWaitEvent(prep_src, fork, 0));
+        GCA_CUDA(ctx, cudaEventRecord(pl->ev_fork_src, main_stream));
+        GCA_CUDA(ctx, cudaStreamWaitEvent(prep_src, pl->ev_fork_src, 0));
+        if (!tracker)
+            GCA_CUDA(ctx, cudaStreamWaitEvent(prep, pl->ev_fork_src, 0));
     }
     ScalePrep sp[GCA3D_MAX_SCALES];
     {
@@ -303,11 +320,21 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         ctx->stream = prep;
         for (int si = 0; si < p.n_scales && !st; ++si)
         {
-            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si], prep_src);
+            // a finer scale's source continues the first scale's sorted state
+            if (!serial && !tracker && si == 1)
+            {
+                const cudaError_t e = cudaStreamWaitEvent(prep, pl->ev_src[0], 0);
+                if (e != cudaSuccess)
+                {
+                    st = cuda_fail(ctx, e, "icp: preparation event");
+                    break;
+                }
+            }
+            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si], src_branch(si) ? prep_src : prep);
             if (!st && !serial)
             {
                 cudaError_t e = cudaEventRecord(pl->ev_scale[si], prep);
-                if (e == cudaSuccess && split)
+                if (e == cudaSuccess && src_branch(si))
                     e = cudaEventRecord(pl->ev_src[si], prep_src);
                 if (e != cudaSuccess)
                     st = cuda_fail(ctx, e, "icp: preparation event");
@@ -316,17 +343,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         ctx->stream = main_stream;
         if (st)
         {
-            if (!serial)
-            {
-                // join the branches before giving up (a capture must end on one stream)
-                cudaEventRecord(pl->ev_fork, prep);
-                cudaStreamWaitEvent(main_stream, pl->ev_fork, 0);
-                if (split)
-                {
-                    cudaEventRecord(pl->ev_fork_src, prep_src);
-                    cudaStreamWaitEvent(main_stream, pl->ev_fork_src, 0);
-                }
-            }
+            join(0);
             return st;
         }
     }
@@ -337,7 +354,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             const gca3d_scale &S = p.scales[si];
             if (!serial)
                 GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
-            if (split)
+            if (src_branch(si))
                 GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_src[si], 0));
             const Batch &bs = sp[si].bs, &bt = sp[si].bt;
             const Grid &gicp = sp[si].gicp;
@@ -432,8 +449,7 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
     if (st && !serial) // join the branches before giving up
     {
         cudaStreamWaitEvent(main_stream, pl->ev_scale[p.n_scales - 1], 0);
-        if (split)
-            cudaStreamWaitEvent(main_stream, pl->ev_src[p.n_scales - 1], 0);
+        cudaStreamWaitEvent(main_stream, pl->ev_src[tracker ? p.n_scales - 1 : 0], 0);
     }
     return st;
 }
@@ -620,7 +636,7 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
                      cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
     for (int k = 0; k < params->n_scales && events_ok; ++k)
         events_ok = cudaEventCreateWithFlags(&pl->ev_scale[k], cudaEventDisableTiming) == cudaSuccess;
-    if (events_ok && pl->vox_given && pl->prologue)
+    if (events_ok)
     {
         events_ok = cudaStreamCreateWithFlags(&pl->prep_src, cudaStreamNonBlocking) == cudaSuccess &&
                     cudaEventCreateWithFlags(&pl->ev_fork_src, cudaEventDisableTiming) == cudaSuccess;
