@@ -410,7 +410,10 @@ def run_ours(args):
     plan_prof.execute(results=True)
     ctx.profile_begin("icp_iter")
     res_prof = plan_prof.execute(results=True)
-    icp_ms, icp_launches = ctx.profile_read()
+    icp_ms, _ = ctx.profile_read()
+    # one launch of the iteration per scale and iteration that some pair ran (the
+    # search and the update are timed as two intervals each)
+    icp_launches = sum(max(r["scale_iterations"][s] for r in res_prof) for s in range(len(SCALES)))
     bytes_total = icp_algorithmic_bytes(res_prof)
     peak, peak_kind = measured_peaks()
     achieved = bytes_total / (icp_ms / 1e3) / 1e9

@@ -381,8 +381,11 @@ __device__ __forceinline__ BlockPair item_pair(int w, const int32_t *src_off, co
 __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restrict__ src_pos, const int32_t *src_off,
                                                         GridDev g, const PairState *st, const int *bmap, int P,
                                                         float max_corr, int2 *corr, NNCerts cert, int32_t *nn_out,
-                                                        int nn_chunk, int *queue)
+                                                        int nn_chunk, int *queue, const int *stop_iter, int stop_at)
 {
+    // a search queued behind the iteration that spent the scale's budget has nothing to do
+    if (stop_iter && *stop_iter >= stop_at)
+        return;
     __shared__ int s_pair, s_w;
     __shared__ float s_T[12];
     __shared__ int s_list[kNNChunkMax];
@@ -837,21 +840,30 @@ int icp_state_init(gca3d_context *ctx, PairState *st, int P, const double *d_Tin
     return GCA3D_OK;
 }
 
-int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
-                  PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
-                  int2 *corr, const NNCerts &cert, const IcpScale &prm, bool compensated, int32_t *nn_out,
-                  const IcpLoop &loop, const IcpShape &shape)
+int icp_search(gca3d_context *ctx, const Batch &src, const Grid &g, PairState *st, int *bmap_nn, int max_blocks_nn,
+               int2 *corr, const NNCerts &cert, const IcpScale &prm, int32_t *nn_out, const IcpLoop *guard,
+               const IcpShape &shape)
+{
+    // work-item loop: enough blocks to fill the SMs a few times over, never more than
+    // the items the capacity can produce
+    const int grid_nn = std::max(std::min(max_blocks_nn, ctx->num_sms * shape.nn_bps), 1);
+    GCA_PROF_BEGIN(ctx, kKidIcpIter);
+    k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
+                                                       corr, cert, nn_out, shape.nn_chunk, bmap_nn + src.P + 1,
+                                                       guard ? guard->iter : nullptr, guard ? guard->max_iter : 0);
+    GCA_CHECK_LAUNCH(ctx);
+    GCA_PROF_END(ctx, kKidIcpIter);
+    return GCA3D_OK;
+}
+
+int icp_update(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
+               PairState *st, int *bmap, int max_blocks, int *bmap_nn, double *partials, const int2 *corr,
+               const IcpScale &prm, bool compensated, const IcpLoop &loop, const IcpShape &shape)
 {
     if (!loop.ticket)
         return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: iteration without a finalize ticket");
-    // work-item loops: enough blocks to fill the SMs a few times over, never more
-    // than the items the capacity can produce
-    const int grid_nn = std::max(std::min(max_blocks_nn, ctx->num_sms * shape.nn_bps), 1);
     const int grid_acc = std::max(std::min(max_blocks, ctx->num_sms * shape.acc_bps), 1);
     GCA_PROF_BEGIN(ctx, kKidIcpIter);
-    k_icp_nn<<<grid_nn, kIcpThreads, 0, ctx->stream>>>(src.pos, src.seg_off, g.dev, st, bmap_nn, src.P, prm.max_corr,
-                                                       corr, cert, nn_out, shape.nn_chunk, bmap_nn + src.P + 1);
-    GCA_CHECK_LAUNCH(ctx);
     const int32_t *d_nt = g.dev.d_n;
     if (shape.fused)
     {
@@ -886,6 +898,20 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
     }
     GCA_PROF_END(ctx, kKidIcpIter);
     return GCA3D_OK;
+}
+
+int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
+                  PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
+                  int2 *corr, const NNCerts &cert, const IcpScale &prm, bool compensated, int32_t *nn_out,
+                  const IcpLoop &loop, const IcpShape &shape)
+{
+    if (!loop.ticket)
+        return fail(ctx, GCA3D_ERR_INVALID_VALUE, "icp: iteration without a finalize ticket");
+    int st_ = icp_search(ctx, src, g, st, bmap_nn, max_blocks_nn, corr, cert, prm, nn_out, nullptr, shape);
+    if (!st_)
+        st_ = icp_update(ctx, src, g, attr0, attr1, st, bmap, max_blocks, bmap_nn, partials, corr, prm, compensated,
+                         loop, shape);
+    return st_;
 }
 
 // ---------------------------------------------------------------------------

@@ -95,6 +95,15 @@ int icp_iteration(gca3d_context *ctx, const Batch &src, const Grid &g, const flo
                   PairState *st, int *bmap, int max_blocks, int *bmap_nn, int max_blocks_nn, double *partials,
                   int2 *corr, const NNCerts &cert, const IcpScale &prm, bool compensated, int32_t *nn_out,
                   const IcpLoop &loop, const IcpShape &shape);
+// the two halves of an iteration: the correspondence search (skipped on the device when
+// guard is given and its iteration count has reached the budget), and the accumulation
+// with the solve and pose update
+int icp_search(gca3d_context *ctx, const Batch &src, const Grid &g, PairState *st, int *bmap_nn, int max_blocks_nn,
+               int2 *corr, const NNCerts &cert, const IcpScale &prm, int32_t *nn_out, const IcpLoop *guard,
+               const IcpShape &shape);
+int icp_update(gca3d_context *ctx, const Batch &src, const Grid &g, const float4 *attr0, const float4 *attr1,
+               PairState *st, int *bmap, int max_blocks, int *bmap_nn, double *partials, const int2 *corr,
+               const IcpScale &prm, bool compensated, const IcpLoop &loop, const IcpShape &shape);
 int build_gn(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,
              double *out30);
 int abs_residual(gca3d_context *ctx, const gca3d_cloud *src, const gca3d_cloud *tgt, const int32_t *nn, float lambda,

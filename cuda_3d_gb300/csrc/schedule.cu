@@ -55,6 +55,7 @@ struct gca3d_icp_plan
     cudaStream_t prep = nullptr;
     cudaEvent_t ev_fork = nullptr;
     cudaEvent_t ev_scale[GCA3D_MAX_SCALES] = {};
+    cudaEvent_t ev_grid[GCA3D_MAX_SCALES] = {}; // the scale's search grid is built (before its normals)
     // the source preparation's branch (the first scale's; every scale's in a tracker plan,
     // where the prologue makes the new frame and the target is the previous one)
     cudaStream_t prep_src = nullptr;
@@ -139,10 +140,11 @@ struct ScalePrep
 };
 
 // one scale's clouds, grids, normals, gradients and iteration scratch, enqueued on the
-// context stream (the source's on src_stream); none of it depends on the pose, so it can
-// run ahead of the iterations
+// context stream (the source's on src_stream; grid_ready, if given, recorded once the
+// search grid is built); none of it depends on the pose, so it can run ahead of the
+// iterations
 static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, VoxelChain &chain_tgt, ScalePrep &out,
-                         cudaStream_t src_stream)
+                         cudaStream_t src_stream, cudaEvent_t grid_ready)
 {
     gca3d_context *ctx = pl->ctx;
     const gca3d_icp_params &p = pl->prm;
@@ -205,6 +207,8 @@ static int prepare_scale(gca3d_icp_plan *pl, int si, VoxelChain &chain_src, Voxe
     if (own_nn_grid && (st = grid_build(ctx, bt, S.max_corr, kOriginPadF32, nullptr, gnn)))
         return st;
     out.gicp = own_nn_grid ? gnn : g;
+    if (grid_ready) // the first correspondence search needs the grid, not the normals
+        GCA_CUDA(ctx, cudaEventRecord(grid_ready, ctx->stream));
     float4 *attr0 = out.attr0 = ctx->arena.get<float4>(g.cap);
     float4 *attr1 = out.attr1 = ctx->arena.get<float4>(g.cap);
     double *partials = out.partials = ctx->arena.get<double>((size_t)std::max(pl->max_blocks, 1) * kTermsPad);
@@ -330,7 +334,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
                     break;
                 }
             }
-            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si], src_branch(si) ? prep_src : prep);
+            st = prepare_scale(pl, si, chain_src, chain_tgt, sp[si], src_branch(si) ? prep_src : prep,
+                               serial ? nullptr : pl->ev_grid[si]);
             if (!st && !serial)
             {
                 cudaError_t e = cudaEventRecord(pl->ev_scale[si], prep);
@@ -352,8 +357,10 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
         for (int si = 0; si < p.n_scales; ++si)
         {
             const gca3d_scale &S = p.scales[si];
+            // the first search waits for the clouds and the search grid, the iterations
+            // for the normals and gradients too
             if (!serial)
-                GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
+                GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_grid[si], 0));
             if (src_branch(si))
                 GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_src[si], 0));
             const Batch &bs = sp[si].bs, &bt = sp[si].bt;
@@ -380,6 +387,12 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             GCA_CUDA(ctx, cudaMemsetAsync(iter, 0, 2 * sizeof(int), ctx->stream));
             IcpLoop loop;
             loop.ticket = reinterpret_cast<unsigned *>(iter + 1);
+            if (S.max_iter > 0 &&
+                (st = icp_search(ctx, bs, gicp, pl->d_state, bmap_nn, pl->max_blocks_nn, corr, cert, prm, nullptr,
+                                 nullptr, shape)))
+                return st;
+            if (!serial)
+                GCA_CUDA(ctx, cudaStreamWaitEvent(main_stream, pl->ev_scale[si], 0));
             if (capturing && S.max_iter > 0)
             {
                 // the iteration loop as a device-side WHILE node: the body runs while a
@@ -406,9 +419,13 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
                 loop.handle = handle;
                 loop.iter = iter;
                 loop.max_iter = S.max_iter;
-                st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                                   pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr, loop,
-                                   shape);
+                // the body: this iteration's update, then the next iteration's search
+                // (which returns at once once the budget is spent)
+                st = icp_update(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn, partials,
+                                corr, prm, p.compensated != 0, loop, shape);
+                if (!st)
+                    st = icp_search(ctx, bs, gicp, pl->d_state, bmap_nn, pl->max_blocks_nn, corr, cert, prm,
+                                    nullptr, &loop, shape);
                 pl->kernels_static -= ctx->launches - l0; // counted per iteration instead
                 ctx->stream = main_stream;
                 cudaGraph_t captured = nullptr;
@@ -425,9 +442,8 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
             }
             for (int it = 0; it < S.max_iter; ++it)
             {
-                if ((st = icp_iteration(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
-                                        pl->max_blocks_nn, partials, corr, cert, prm, p.compensated != 0, nullptr,
-                                        loop, shape)))
+                if ((st = icp_update(ctx, bs, gicp, attr0, attr1, pl->d_state, bmap, pl->max_blocks, bmap_nn,
+                                     partials, corr, prm, p.compensated != 0, loop, shape)))
                     return st;
                 if (pl->host_checks && !capturing)
                 {
@@ -440,6 +456,10 @@ int run_schedule(gca3d_icp_plan *pl, bool capturing)
                     if (!any)
                         break;
                 }
+                if (it + 1 < S.max_iter &&
+                    (st = icp_search(ctx, bs, gicp, pl->d_state, bmap_nn, pl->max_blocks_nn, corr, cert, prm,
+                                     nullptr, nullptr, shape)))
+                    return st;
             }
         }
 
@@ -521,6 +541,9 @@ int gca3d_icp_plan_destroy(gca3d_icp_plan *pl)
     if (pl->ev_fork_src)
         cudaEventDestroy(pl->ev_fork_src);
     for (cudaEvent_t e : pl->ev_src)
+        if (e)
+            cudaEventDestroy(e);
+    for (cudaEvent_t e : pl->ev_grid)
         if (e)
             cudaEventDestroy(e);
     if (pl->ev_fork)
@@ -635,7 +658,8 @@ int gca3d::icp_plan_create_internal(gca3d_context *ctx, int P, gca3d_cloud *cons
     bool events_ok = cudaStreamCreateWithFlags(&pl->prep, cudaStreamNonBlocking) == cudaSuccess &&
                      cudaEventCreateWithFlags(&pl->ev_fork, cudaEventDisableTiming) == cudaSuccess;
     for (int k = 0; k < params->n_scales && events_ok; ++k)
-        events_ok = cudaEventCreateWithFlags(&pl->ev_scale[k], cudaEventDisableTiming) == cudaSuccess;
+        events_ok = cudaEventCreateWithFlags(&pl->ev_scale[k], cudaEventDisableTiming) == cudaSuccess &&
+                    cudaEventCreateWithFlags(&pl->ev_grid[k], cudaEventDisableTiming) == cudaSuccess;
     if (events_ok)
     {
         events_ok = cudaStreamCreateWithFlags(&pl->prep_src, cudaStreamNonBlocking) == cudaSuccess &&
