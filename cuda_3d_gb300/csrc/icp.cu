@@ -514,8 +514,8 @@ __global__ void __launch_bounds__(kIcpThreads, 5) k_icp_nn(const float4 *__restr
 // reference's convergence test (color_icp.cu:216-228).  The partials are read from
 // L2: in the fused accumulate other blocks of the same launch wrote them.
 template <bool Comp>
-__device__ __noinline__ void finalize_pair(PairState *st, int P, int pair, const int *bmap, const double *partials,
-                                           IcpScale prm)
+__device__ __forceinline__ void finalize_pair_body(PairState *st, int P, int pair, const int *bmap,
+                                                   const double *partials, const IcpScale &prm)
 {
     PairState &Ps = st[pair];
     __shared__ double s_red[kIcpThreads / 32][kTermsPad];
@@ -642,7 +642,7 @@ __device__ __noinline__ void finalize_pair(PairState *st, int P, int pair, const
 // launches get no items for converged pairs), their count and, in a captured
 // schedule, the loop condition.  Run by one whole block once every pair of the
 // iteration is finalized.
-__device__ __noinline__ void rebuild_maps(PairState *st, int P, int *bmap, int *bmap_nn, IcpLoop loop)
+__device__ __forceinline__ void rebuild_maps_body(PairState *st, int P, int *bmap, int *bmap_nn, const IcpLoop &loop)
 {
     __shared__ int s_nact;
     if (threadIdx.x == 0)
@@ -685,6 +685,21 @@ __device__ __noinline__ void rebuild_maps(PairState *st, int P, int *bmap, int *
             an += st[q].nblocks_nn;
         }
     }
+}
+
+// the same two steps as calls, for the fused accumulate: compiled apart from the
+// accumulation loop, whose registers they would otherwise crowd (the separate finalize
+// kernel inlines the bodies)
+template <bool Comp>
+__device__ __noinline__ void finalize_pair(PairState *st, int P, int pair, const int *bmap, const double *partials,
+                                           IcpScale prm)
+{
+    finalize_pair_body<Comp>(st, P, pair, bmap, partials, prm);
+}
+
+__device__ __noinline__ void rebuild_maps(PairState *st, int P, int *bmap, int *bmap_nn, IcpLoop loop)
+{
+    rebuild_maps_body(st, P, bmap, bmap_nn, loop);
 }
 
 // step 2: residuals, Jacobians, block sums (one partial per block); three resident
@@ -796,7 +811,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
 {
     __shared__ int s_last;
     if (st[blockIdx.x].active)
-        finalize_pair<Comp>(st, P, blockIdx.x, bmap, partials, prm);
+        finalize_pair_body<Comp>(st, P, blockIdx.x, bmap, partials, prm);
     if (gridDim.x > 1)
     {
         __threadfence();
@@ -809,7 +824,7 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp_finalize(PairState *st, int
     __syncthreads();
     if (!s_last)
         return;
-    rebuild_maps(st, P, bmap, bmap_nn, loop);
+    rebuild_maps_body(st, P, bmap, bmap_nn, loop);
 }
 
 IcpShape icp_shape(const gca3d_tuning &t)
