@@ -270,7 +270,8 @@ __device__ __forceinline__ void sort_tile(const TileJob &J, SortCtl *ctl, const 
                                           uint64_t *s_keys, int32_t *s_vals, uint32_t *s_wsum)
 {
     const uint32_t tile = J.tile;
-    const int first = J.first, seg = J.seg, seg_b = J.seg_b, seg_e = J.seg_e, tile_base = J.tile_base, cnt = J.cnt;
+    const int first = J.first, seg = J.seg, tile_base = J.tile_base, cnt = J.cnt;
+    [[maybe_unused]] const int seg_b = J.seg_b, seg_e = J.seg_e; // the checked build's index checks
     const int shift = J.shift, pass = J.pass;
     const uint64_t *kin = J.kin;
     const int32_t *vin = J.vin;
